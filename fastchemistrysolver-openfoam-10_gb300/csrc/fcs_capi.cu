@@ -1,0 +1,561 @@
+// fcs_capi.cu -- the C ABI of libfcs_cuda.so (include/fcs.h): context and
+// device-memory management, mechanism packing, launch-shape selection
+// (autotuner) and the batched integrate / rhs / jacobian / rates entry points.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/fcs.h"
+#include "fcs_device.cuh"
+#include "fcs_internal.h"
+#include "fcs_launch.h"
+
+using namespace fcs;
+
+namespace {
+
+template<class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t ensure(size_t want) {
+        if (want <= n) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(want, 1) * sizeof(T));
+        if (e == cudaSuccess) n = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct Shape {
+    LaunchCfg lc;
+    SlotLayout L;
+    bool global;      // workspace in global memory
+    bool mixed;
+};
+
+}  // namespace
+
+struct fcs_ctx {
+    int device = 0;
+    int numSMs = 0;
+    size_t maxSmemPerBlock = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string err;
+    // mechanism
+    bool loaded = false;
+    DevMech M{};
+    DBuf<double> dW, dInvW, dTc, dCoef, dEff, dPlogRow, dPlogTa, dHf;
+    DBuf<RxnInfo> dRx;
+    DBuf<int> dPlogOff, dIncOff, dInc;
+    // options
+    fcs_options opt{};
+    // per-call buffers
+    DBuf<double> bp, brho, bT, bY, bSub, bRR, bDt, bOut, bJ, bQ;
+    DBuf<int> bStatus, bOrder, bHead;
+    DBuf<long long> bStats;
+    DBuf<unsigned long long> bMin;
+    DBuf<char> gws;
+    std::map<std::tuple<int, int, int, int>, int> tuned;  // (n, precision, solver, jac) -> group
+};
+
+static fcs_status set_err(fcs_ctx* c, fcs_status s, const std::string& m) {
+    if (c) c->err = m;
+    return s;
+}
+
+static fcs_status cuda_err(fcs_ctx* c, cudaError_t e, const char* where) {
+    return set_err(c, FCS_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                                  \
+    do {                                                          \
+        cudaError_t e_ = (call);                                  \
+        if (e_ != cudaSuccess) return cuda_err(ctx, e_, #call);   \
+    } while (0)
+
+extern "C" const char* fcs_version(void) { return "fcs-gb300 1.0 (sm_103a)"; }
+
+extern "C" fcs_status fcs_default_options(fcs_options* o) {
+    if (!o) return FCS_ERR_INVALID;
+    o->solver = FCS_SOLVER_RODAS34;
+    o->jacobian = FCS_JACOBIAN_EXACT;
+    o->precision = FCS_PRECISION_FP64;
+    o->mapping = FCS_MAPPING_AUTO;
+    o->abs_tol = 1e-8;
+    o->rel_tol = 1e-4;
+    o->max_steps = 10000;
+    o->max_rejects = 1000;
+    o->T_react = 0.0;
+    o->delta_t_chem_max = 1e300;
+    return FCS_OK;
+}
+
+extern "C" fcs_status fcs_create(fcs_ctx** out, int device) {
+    if (!out) return FCS_ERR_INVALID;
+    *out = nullptr;
+    fcs_ctx* ctx = new fcs_ctx();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { delete ctx; return FCS_ERR_CUDA; }
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device);
+    ctx->numSMs = v;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    ctx->maxSmemPerBlock = (size_t)v;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+        delete ctx;
+        return FCS_ERR_CUDA;
+    }
+    fcs_default_options(&ctx->opt);
+    *out = ctx;
+    return FCS_OK;
+}
+
+extern "C" fcs_status fcs_destroy(fcs_ctx* ctx) {
+    if (!ctx) return FCS_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (DBuf<double>* b : {&ctx->dW, &ctx->dInvW, &ctx->dTc, &ctx->dCoef, &ctx->dEff, &ctx->dPlogRow,
+                            &ctx->dPlogTa, &ctx->dHf, &ctx->bp, &ctx->brho, &ctx->bT, &ctx->bY,
+                            &ctx->bSub, &ctx->bRR, &ctx->bDt, &ctx->bOut, &ctx->bJ, &ctx->bQ})
+        b->release();
+    ctx->dRx.release();
+    ctx->dPlogOff.release(); ctx->dIncOff.release(); ctx->dInc.release();
+    ctx->bStatus.release(); ctx->bOrder.release(); ctx->bHead.release();
+    ctx->bStats.release(); ctx->bMin.release(); ctx->gws.release();
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return FCS_OK;
+}
+
+extern "C" const char* fcs_last_error_string(const fcs_ctx* ctx) {
+    return ctx ? ctx->err.c_str() : "null context";
+}
+
+extern "C" fcs_status fcs_set_options(fcs_ctx* ctx, const fcs_options* o) {
+    if (!ctx || !o) return FCS_ERR_INVALID;
+    if (o->solver < 0 || o->solver > 2) return set_err(ctx, FCS_ERR_INVALID, "solver must be 0..2");
+    if (o->jacobian < 0 || o->jacobian > 1) return set_err(ctx, FCS_ERR_INVALID, "jacobian must be exact or fast");
+    if (o->precision < 0 || o->precision > 1) return set_err(ctx, FCS_ERR_INVALID, "precision must be fp64 or mixed");
+    if (!(o->abs_tol > 0) || !(o->rel_tol > 0)) return set_err(ctx, FCS_ERR_INVALID, "tolerances must be positive");
+    if (o->max_steps <= 0 || o->max_rejects <= 0) return set_err(ctx, FCS_ERR_INVALID, "maxSteps must be positive");
+    const int m = o->mapping;
+    if (m != 0 && m != 32 && m != 64 && m != 128 && m != 256)
+        return set_err(ctx, FCS_ERR_INVALID, "mapping must be auto, 32, 64, 128 or 256");
+    ctx->opt = *o;
+    return FCS_OK;
+}
+
+extern "C" fcs_status fcs_mechanism_size(const fcs_ctx* ctx, int32_t* ns, int32_t* nr) {
+    if (!ctx || !ctx->loaded) return FCS_ERR_STATE;
+    if (ns) *ns = ctx->M.ns;
+    if (nr) *nr = ctx->M.nr;
+    return FCS_OK;
+}
+
+// ------------------------------------------------------------------------
+// mechanism packing: type-block order of OptReaction::readInfo
+// (OptReaction.C:448-1175), species incidence lists in reaction order.
+
+extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc* d) {
+    if (!ctx || !d) return FCS_ERR_INVALID;
+    const int ns = d->n_species, nr = d->n_reactions;
+    if (ns < 1 || nr < 0 || ns > 32000) return set_err(ctx, FCS_ERR_INVALID, "bad species/reaction count");
+    if (!d->W || !d->T_low || !d->T_high || !d->T_common || !d->high_coeffs || !d->low_coeffs)
+        return set_err(ctx, FCS_ERR_INVALID, "missing species arrays");
+    if (nr > 0 && (!d->type || !d->reversible || !d->lhs_offset || !d->lhs_species || !d->rhs_offset ||
+                   !d->rhs_species || !d->arrhenius))
+        return set_err(ctx, FCS_ERR_INVALID, "missing reaction arrays");
+    std::vector<int> order;
+    for (int pass = 0; pass < 4; pass++) {
+        for (int r = 0; r < nr; r++) {
+            const int t = d->type[r];
+            const bool tind = d->arrhenius[3 * r + 1] == 0 && d->arrhenius[3 * r + 2] == 0;
+            if ((pass == 0 && t == FCS_RXN_ARRHENIUS && tind) || (pass == 1 && t == FCS_RXN_ARRHENIUS && !tind) ||
+                (pass == 2 && t == FCS_RXN_THIRD_BODY) || (pass == 3 && t == FCS_RXN_PLOG))
+                order.push_back(r);
+        }
+    }
+    if ((int)order.size() != nr)
+        return set_err(ctx, FCS_ERR_UNSUPPORTED,
+                       "reaction types other than (ir)reversible Arrhenius, ThirdBodyArrhenius and "
+                       "ArrheniusPLOG are not supported by the GPU path");
+    std::vector<double> W(ns), invW(ns), Tc(ns), coef(16 * (size_t)ns, 0.0), hf(ns);
+    double TlowMin = 1e10, ThighMax = 1, TcMin = 1e10, TcMax = 0;
+    for (int i = 0; i < ns; i++) {
+        if (!(d->W[i] > 0)) return set_err(ctx, FCS_ERR_INVALID, "molecular weight must be positive");
+        W[i] = d->W[i];
+        invW[i] = 1.0 / d->W[i];
+        Tc[i] = d->T_common[i];
+        for (int j = 0; j < 7; j++) {
+            coef[16 * i + j] = d->low_coeffs[7 * i + j];
+            coef[16 * i + 8 + j] = d->high_coeffs[7 * i + j];
+        }
+        TlowMin = std::min(TlowMin, d->T_low[i]);
+        ThighMax = std::max(ThighMax, d->T_high[i]);
+        TcMin = std::min(TcMin, d->T_common[i]);
+        TcMax = std::max(TcMax, d->T_common[i]);
+        // formation enthalpy at Tstd = 298.15 K (janaf Hf), J/kg
+        const double* a = (298.15 < d->T_common[i]) ? &d->low_coeffs[7 * i] : &d->high_coeffs[7 * i];
+        const double T = 298.15;
+        hf[i] = kRu * invW[i] *
+                (((((a[4] / 5 * T + a[3] / 4) * T + a[2] / 3) * T + a[1] / 2) * T + a[0]) * T + a[5]);
+    }
+    std::vector<RxnInfo> rx(std::max(nr, 1));
+    std::vector<double> eff;
+    std::vector<int> plogOff{0};
+    std::vector<double> plogRow, plogTa;
+    std::vector<std::vector<int>> inc(ns);
+    int nTB = 0, nPlog = 0;
+    for (int k = 0; k < nr; k++) {
+        const int r = order[k];
+        RxnInfo& x = rx[k];
+        std::memset(&x, 0, sizeof(x));
+        x.A = d->arrhenius[3 * r];
+        x.beta = d->arrhenius[3 * r + 1];
+        x.Ta = d->arrhenius[3 * r + 2];
+        const int l0 = d->lhs_offset[r], l1 = d->lhs_offset[r + 1];
+        const int r0 = d->rhs_offset[r], r1 = d->rhs_offset[r + 1];
+        if (l1 - l0 < 1 || r1 - r0 < 1)
+            return set_err(ctx, FCS_ERR_INVALID, "reaction without reactants or products");
+        if (l1 - l0 > kMaxSide || r1 - r0 > kMaxSide)
+            return set_err(ctx, FCS_ERR_UNSUPPORTED, "reactions with more than 3 reactants or products "
+                                                     "(the reference's RFG/JFG path) are not supported");
+        x.nl = int8_t(l1 - l0);
+        x.nr = int8_t(r1 - r0);
+        for (int q = 0; q < x.nl; q++) {
+            const int sp = d->lhs_species[l0 + q];
+            if (sp < 0 || sp >= ns) return set_err(ctx, FCS_ERR_INVALID, "species index out of range");
+            x.sl[q] = int16_t(sp);
+            inc[sp].push_back(k << 1);
+        }
+        for (int q = 0; q < x.nr; q++) {
+            const int sp = d->rhs_species[r0 + q];
+            if (sp < 0 || sp >= ns) return set_err(ctx, FCS_ERR_INVALID, "species index out of range");
+            x.sr[q] = int16_t(sp);
+            inc[sp].push_back((k << 1) | 1);
+        }
+        x.rev = d->reversible[r] ? 1 : 0;
+        x.kind = int8_t(d->type[r]);
+        x.dnu = x.nr - x.nl;
+        x.tind = (x.beta == 0 && x.Ta == 0) ? 1 : 0;
+        x.tb = -1;
+        x.plog = -1;
+        if (d->type[r] == FCS_RXN_THIRD_BODY) {
+            if (!d->efficiencies) return set_err(ctx, FCS_ERR_INVALID, "third-body reaction without efficiencies");
+            for (int s = 0; s < ns; s++) eff.push_back(d->efficiencies[(size_t)r * ns + s]);
+            x.tb = nTB++;
+        }
+        if (d->type[r] == FCS_RXN_PLOG) {
+            if (!d->plog_offset || !d->plog_table) return set_err(ctx, FCS_ERR_INVALID, "PLOG reaction without table");
+            const int q0 = d->plog_offset[r], q1 = d->plog_offset[r + 1];
+            if (q1 - q0 < 1) return set_err(ctx, FCS_ERR_INVALID, "empty PLOG table");
+            for (int q = q0; q < q1; q++) {
+                const double* row = &d->plog_table[4 * (size_t)q];
+                if (!(row[0] > 0) || !(row[1] > 0)) return set_err(ctx, FCS_ERR_INVALID, "PLOG p and A must be positive");
+                plogRow.push_back(row[0]);
+                plogRow.push_back(std::log(row[0]));
+                plogRow.push_back(std::log(row[1]));
+                plogRow.push_back(row[2]);
+                plogTa.push_back(row[3]);
+            }
+            plogOff.push_back(plogOff.back() + (q1 - q0));
+            x.plog = nPlog++;
+        }
+    }
+    std::vector<int> incOff(ns + 1, 0), incv;
+    for (int i = 0; i < ns; i++) {
+        incOff[i + 1] = incOff[i] + (int)inc[i].size();
+        incv.insert(incv.end(), inc[i].begin(), inc[i].end());
+    }
+    if (incv.empty()) incv.push_back(0);
+    if (eff.empty()) eff.push_back(0);
+    if (plogRow.empty()) { plogRow.assign(4, 0); plogTa.assign(1, 0); }
+    cudaSetDevice(ctx->device);
+    auto up = [&](auto& buf, const auto& v) -> cudaError_t {
+        cudaError_t e = buf.ensure(v.size());
+        if (e != cudaSuccess) return e;
+        return cudaMemcpy(buf.p, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice);
+    };
+    CK(up(ctx->dW, W)); CK(up(ctx->dInvW, invW)); CK(up(ctx->dTc, Tc)); CK(up(ctx->dCoef, coef));
+    CK(up(ctx->dRx, rx)); CK(up(ctx->dEff, eff)); CK(up(ctx->dPlogOff, plogOff));
+    CK(up(ctx->dPlogRow, plogRow)); CK(up(ctx->dPlogTa, plogTa)); CK(up(ctx->dIncOff, incOff));
+    CK(up(ctx->dInc, incv)); CK(up(ctx->dHf, hf));
+    DevMech& M = ctx->M;
+    M.ns = ns; M.n = ns + 1; M.nr = nr; M.nTB = nTB; M.nPlog = nPlog;
+    M.TlowMin = TlowMin; M.ThighMax = ThighMax; M.TcommonMin = TcMin; M.TcommonMax = TcMax;
+    M.W = ctx->dW.p; M.invW = ctx->dInvW.p; M.Tcommon = ctx->dTc.p; M.coef = ctx->dCoef.p;
+    M.rx = ctx->dRx.p; M.eff = ctx->dEff.p; M.plogOff = ctx->dPlogOff.p; M.plogRow = ctx->dPlogRow.p;
+    M.plogTa = ctx->dPlogTa.p; M.incOff = ctx->dIncOff.p; M.inc = ctx->dInc.p; M.hf = ctx->dHf.p;
+    ctx->loaded = true;
+    ctx->tuned.clear();
+    return FCS_OK;
+}
+
+// ------------------------------------------------------------------------
+// launch shapes
+
+static KOpts kopts(const fcs_options& o) {
+    KOpts k;
+    k.solver = o.solver;
+    k.jacobian = o.jacobian;
+    k.maxSteps = o.max_steps;
+    k.maxRejects = o.max_rejects;
+    k.absTol = o.abs_tol;
+    k.relTol = o.rel_tol;
+    k.Treact = o.T_react;
+    k.dtChemMax = o.delta_t_chem_max;
+    return k;
+}
+
+// Build the launch shape for a group size; returns false when impossible.
+static bool make_shape(fcs_ctx* ctx, int group, bool integrate, Shape& sh) {
+    const fcs_options& o = ctx->opt;
+    const bool mixed = o.precision == FCS_PRECISION_MIXED;
+    const bool seulex = integrate && o.solver == FCS_SOLVER_SEULEX;
+    const bool two = mixed || seulex;
+    sh.mixed = mixed;
+    sh.L = make_layout(ctx->M.ns, ctx->M.nr, ctx->M.nTB, mixed ? 4 : 8, two, seulex);
+    sh.lc.group = group;
+    if (group == 32 && ctx->M.n > 256) return false;  // warp solves keep <= 256 unknowns in registers
+    const size_t smemCap = ctx->maxSmemPerBlock;
+    int groupsPerBlock = 1;
+    if (group == 32) {
+        groupsPerBlock = (int)std::min<size_t>(8, smemCap / (size_t)sh.L.bytes);
+        if (groupsPerBlock < 1) groupsPerBlock = 1;
+    }
+    sh.global = (size_t)sh.L.bytes > smemCap;
+    sh.lc.block = group * groupsPerBlock;
+    int maxThreads = 0, regs = 0;
+    if (integrate_attributes(group, mixed, &maxThreads, &regs) != cudaSuccess) return false;
+    if (sh.lc.block > maxThreads) return false;
+    // resident blocks per SM: shared memory and registers
+    int perSM = 1;
+    if (!sh.global) {
+        const size_t perBlock = (size_t)sh.L.bytes * groupsPerBlock + 1024;
+        perSM = (int)std::max<size_t>(1, (228 * 1024) / perBlock);
+    } else {
+        perSM = 2;
+    }
+    const int regLimit = std::max(1, 65536 / std::max(1, regs * sh.lc.block));
+    perSM = std::max(1, std::min(perSM, regLimit));
+    sh.lc.grid = ctx->numSMs * perSM;
+    return true;
+}
+
+static fcs_status ensure_gws(fcs_ctx* ctx, const Shape& sh) {
+    if (!sh.global) return FCS_OK;
+    const size_t groups = (size_t)sh.lc.grid * (sh.lc.block / sh.lc.group);
+    if (ctx->gws.ensure(groups * (size_t)sh.L.bytes) != cudaSuccess)
+        return set_err(ctx, FCS_ERR_NOMEM, "global workspace allocation failed");
+    return FCS_OK;
+}
+
+static int default_group(fcs_ctx* ctx) {
+    const int n = ctx->M.n;
+    if (n <= 64) return 32;
+    if (n <= 128) return 64;
+    return 128;
+}
+
+// ------------------------------------------------------------------------
+// integration
+
+static fcs_status integrate_impl(fcs_ctx* ctx, int64_t nc, double dt, const double* dtc,
+                                 const double* p, const double* rho0, double* T, double* Y,
+                                 double* sub, double* RR, int32_t* status, fcs_step_stats* stats,
+                                 double* dtMin, int32_t flags) {
+    if (!ctx) return FCS_ERR_INVALID;
+    if (!ctx->loaded) return set_err(ctx, FCS_ERR_STATE, "no mechanism loaded");
+    if (nc < 0 || nc > (int64_t)INT32_MAX) return set_err(ctx, FCS_ERR_INVALID, "n_cells out of range");
+    if (!p || !rho0 || !T || !Y || !sub) return set_err(ctx, FCS_ERR_INVALID, "null cell array");
+    if (!dtc && !(dt > 0)) return set_err(ctx, FCS_ERR_INVALID, "delta_t must be positive");
+    cudaSetDevice(ctx->device);
+    const int ns = ctx->M.ns;
+    const bool dev = flags & FCS_PTR_DEVICE;
+    cudaStream_t st = ctx->stream;
+    CellIO io{};
+    io.nCells = nc;
+    io.deltaT = dt;
+    if (dev) {
+        io.p = p; io.rho0 = rho0; io.T = T; io.Y = Y; io.subDt = sub; io.RR = RR; io.status = status;
+        io.dtPerCell = dtc;
+    } else {
+        CK(ctx->bp.ensure(nc)); CK(ctx->brho.ensure(nc)); CK(ctx->bT.ensure(nc));
+        CK(ctx->bY.ensure((size_t)ns * nc)); CK(ctx->bSub.ensure(nc)); CK(ctx->bStatus.ensure(nc));
+        if (RR) CK(ctx->bRR.ensure((size_t)ns * nc));
+        if (dtc) CK(ctx->bDt.ensure(nc));
+        CK(cudaMemcpyAsync(ctx->bp.p, p, nc * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(ctx->brho.p, rho0, nc * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(ctx->bT.p, T, nc * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(ctx->bY.p, Y, (size_t)ns * nc * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(ctx->bSub.p, sub, nc * 8, cudaMemcpyHostToDevice, st));
+        if (dtc) CK(cudaMemcpyAsync(ctx->bDt.p, dtc, nc * 8, cudaMemcpyHostToDevice, st));
+        io.p = ctx->bp.p; io.rho0 = ctx->brho.p; io.T = ctx->bT.p; io.Y = ctx->bY.p;
+        io.subDt = ctx->bSub.p; io.RR = RR ? ctx->bRR.p : nullptr; io.status = ctx->bStatus.p;
+        io.dtPerCell = dtc ? ctx->bDt.p : nullptr;
+    }
+    CK(ctx->bStats.ensure(ST_COUNT));
+    CK(ctx->bMin.ensure(1));
+    CK(ctx->bOrder.ensure(std::max<int64_t>(nc, 1)));
+    CK(ctx->bHead.ensure(2));
+    io.stats = ctx->bStats.p;
+    io.dtMinBits = ctx->bMin.p;
+    CK(cudaMemsetAsync(ctx->bStats.p, 0, ST_COUNT * sizeof(long long), st));
+    CK(cudaMemsetAsync(ctx->bMin.p, 0x7f, sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(ctx->bHead.p, 0, 2 * sizeof(int), st));
+    // classify: cells with T <= Treact are skipped (transientSolve.H:39, 70-76)
+    CK(launch_classify(io, ns, ctx->opt.T_react, ctx->bOrder.p, ctx->bHead.p + 1, st));
+    int nActive = 0;
+    CK(cudaMemcpyAsync(&nActive, ctx->bHead.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const int group = ctx->opt.mapping ? ctx->opt.mapping : default_group(ctx);
+    Shape sh;
+    if (!make_shape(ctx, group, true, sh))
+        return set_err(ctx, FCS_ERR_UNSUPPORTED, "no launch shape for this mapping");
+    fcs_status s = ensure_gws(ctx, sh);
+    if (s != FCS_OK) return s;
+    WorkQueue q{ctx->bHead.p, ctx->bOrder.p, nActive};
+    const KOpts ko = kopts(ctx->opt);
+    CK(cudaEventRecord(ctx->ev0, st));
+    if (nActive > 0) CK(launch_integrate(sh.lc, sh.mixed, ctx->M, ko, sh.L, io, q, sh.global ? ctx->gws.p : nullptr, st));
+    CK(cudaEventRecord(ctx->ev1, st));
+    long long hs[ST_COUNT];
+    unsigned long long hmin = 0;
+    CK(cudaMemcpyAsync(hs, ctx->bStats.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&hmin, ctx->bMin.p, sizeof(hmin), cudaMemcpyDeviceToHost, st));
+    if (!dev) {
+        CK(cudaMemcpyAsync(T, io.T, nc * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(Y, io.Y, (size_t)ns * nc * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(sub, io.subDt, nc * 8, cudaMemcpyDeviceToHost, st));
+        if (RR) CK(cudaMemcpyAsync(RR, io.RR, (size_t)ns * nc * 8, cudaMemcpyDeviceToHost, st));
+        if (status) CK(cudaMemcpyAsync(status, io.status, nc * 4, cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    if (stats) {
+        stats->cells_integrated = hs[ST_CELLS];
+        stats->cells_skipped = hs[ST_SKIPPED];
+        stats->cells_failed = hs[ST_FAILED];
+        stats->attempts = hs[ST_ATTEMPTS];
+        stats->accepted = hs[ST_ACCEPTED];
+        stats->jacobians = hs[ST_JAC];
+        stats->lu_decompositions = hs[ST_LU];
+        stats->rhs_evaluations = hs[ST_RHS];
+        stats->linear_solves = hs[ST_SOLVES];
+        stats->kernel_ms = ms;
+    }
+    if (dtMin) {
+        double m = 1e15;  // great
+        if (hs[ST_CELLS] > 0) std::memcpy(&m, &hmin, sizeof(m));
+        const double dref = dtc ? 0 : dt;
+        *dtMin = dtc ? m : std::min(m, 2 * dref);
+    }
+    if (hs[ST_FAILED] > 0) return set_err(ctx, FCS_ERR_CELLS, "some cells failed; see cell_status");
+    return FCS_OK;
+}
+
+extern "C" fcs_status fcs_integrate(fcs_ctx* ctx, int64_t n, double dt, const double* p, const double* rho0,
+                                    double* T, double* Y, double* sub, double* RR, int32_t* status,
+                                    fcs_step_stats* stats, double* dtMin, int32_t flags) {
+    return integrate_impl(ctx, n, dt, nullptr, p, rho0, T, Y, sub, RR, status, stats, dtMin, flags);
+}
+
+extern "C" fcs_status fcs_integrate_lts(fcs_ctx* ctx, int64_t n, const double* dt, const double* p,
+                                        const double* rho0, double* T, double* Y, double* sub, double* RR,
+                                        int32_t* status, fcs_step_stats* stats, double* dtMin, int32_t flags) {
+    if (!dt) return set_err(ctx, FCS_ERR_INVALID, "delta_t array is null");
+    return integrate_impl(ctx, n, 0.0, dt, p, rho0, T, Y, sub, RR, status, stats, dtMin, flags);
+}
+
+// ------------------------------------------------------------------------
+// per-cell evaluations
+
+static fcs_status eval_impl(fcs_ctx* ctx, int64_t nc, const double* p, const double* T, const double* rho,
+                            const double* Y, double* out, double* J, double* Qdot, int mode, int32_t flags) {
+    if (!ctx) return FCS_ERR_INVALID;
+    if (!ctx->loaded) return set_err(ctx, FCS_ERR_STATE, "no mechanism loaded");
+    if (nc < 0 || nc > (int64_t)INT32_MAX) return set_err(ctx, FCS_ERR_INVALID, "n_cells out of range");
+    if (!p || !T || !Y || !out) return set_err(ctx, FCS_ERR_INVALID, "null array");
+    if (nc == 0) return FCS_OK;
+    cudaSetDevice(ctx->device);
+    const int ns = ctx->M.ns, n = ctx->M.n;
+    const bool dev = flags & FCS_PTR_DEVICE;
+    cudaStream_t st = ctx->stream;
+    const size_t nout = (size_t)(mode == 2 ? ns : n) * nc;
+    if (mode == 2 && !rho) return set_err(ctx, FCS_ERR_INVALID, "null rho");
+    const double *dp = p, *dT = T, *dY = Y, *drho = rho;
+    double *dout = out, *dJ = J, *dQ = Qdot;
+    if (!dev) {
+        CK(ctx->bp.ensure(nc)); CK(ctx->bT.ensure(nc)); CK(ctx->bY.ensure((size_t)ns * nc));
+        CK(ctx->bOut.ensure(nout));
+        CK(cudaMemcpyAsync(ctx->bp.p, p, nc * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(ctx->bT.p, T, nc * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(ctx->bY.p, Y, (size_t)ns * nc * 8, cudaMemcpyHostToDevice, st));
+        dp = ctx->bp.p; dT = ctx->bT.p; dY = ctx->bY.p; dout = ctx->bOut.p;
+        if (mode == 2) {
+            CK(ctx->brho.ensure(nc));
+            CK(cudaMemcpyAsync(ctx->brho.p, rho, nc * 8, cudaMemcpyHostToDevice, st));
+            drho = ctx->brho.p;
+        }
+        if (J) { CK(ctx->bJ.ensure((size_t)n * n * nc)); dJ = ctx->bJ.p; }
+        if (Qdot) { CK(ctx->bQ.ensure(nc)); dQ = ctx->bQ.p; }
+    }
+    const int group = default_group(ctx);
+    Shape sh;
+    if (!make_shape(ctx, group, false, sh)) return set_err(ctx, FCS_ERR_UNSUPPORTED, "no launch shape");
+    const int gpb = sh.lc.block / sh.lc.group;
+    sh.lc.grid = (int)((nc + gpb - 1) / gpb);
+    char* gws = nullptr;
+    if (sh.global) {
+        if (ctx->gws.ensure((size_t)sh.lc.grid * gpb * sh.L.bytes) != cudaSuccess)
+            return set_err(ctx, FCS_ERR_NOMEM, "workspace allocation failed");
+        gws = ctx->gws.p;
+    }
+    const KOpts ko = kopts(ctx->opt);
+    CK(launch_eval(sh.lc, sh.mixed, ctx->M, ko, sh.L, nc, dp, dT, drho, dY, dout, dJ, dQ, mode, gws, st));
+    if (!dev) {
+        CK(cudaMemcpyAsync(out, dout, nout * 8, cudaMemcpyDeviceToHost, st));
+        if (J) CK(cudaMemcpyAsync(J, dJ, (size_t)n * n * nc * 8, cudaMemcpyDeviceToHost, st));
+        if (Qdot) CK(cudaMemcpyAsync(Qdot, dQ, nc * 8, cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaStreamSynchronize(st));
+    return FCS_OK;
+}
+
+extern "C" fcs_status fcs_rhs(fcs_ctx* ctx, int64_t n, const double* p, const double* T, const double* Y,
+                              double* dydt, int32_t flags) {
+    return eval_impl(ctx, n, p, T, nullptr, Y, dydt, nullptr, nullptr, 0, flags);
+}
+
+extern "C" fcs_status fcs_jacobian(fcs_ctx* ctx, int64_t n, const double* p, const double* T, const double* Y,
+                                   double* J, double* dydt, int32_t flags) {
+    if (!J) return set_err(ctx, FCS_ERR_INVALID, "null J");
+    return eval_impl(ctx, n, p, T, nullptr, Y, dydt, J, nullptr, 1, flags);
+}
+
+extern "C" fcs_status fcs_rates(fcs_ctx* ctx, int64_t n, const double* p, const double* T, const double* rho,
+                                const double* Y, double* RR, double* Qdot, int32_t flags) {
+    return eval_impl(ctx, n, p, T, rho, Y, RR, nullptr, Qdot, 2, flags);
+}

@@ -1,0 +1,68 @@
+// fcs_dispatch.cu -- run-time dispatch over the per-group-size kernel
+// instantiations, and the cell classification kernel.
+#include "fcs_kernels.cuh"
+
+namespace fcs {
+
+// Treact skip + compaction of the active cells into the work queue
+__global__ void classify_kernel(CellIO io, int ns, double Treact, int* order, int* count) {
+    const long long nc = io.nCells;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < nc;
+         c += (long long)gridDim.x * blockDim.x) {
+        if (io.T[c] > Treact) {
+            const int k = atomicAdd(count, 1);
+            order[k] = (int)c;
+        } else {
+            if (io.RR) for (int i = 0; i < ns; i++) io.RR[(size_t)i * nc + c] = 0;
+            if (io.status) io.status[c] = FCS_CELL_SKIPPED;
+            atomicAdd(reinterpret_cast<unsigned long long*>(&io.stats[ST_SKIPPED]), 1ull);
+        }
+    }
+}
+
+cudaError_t launch_integrate(const LaunchCfg& lc, bool mixed, const DevMech& M, const KOpts& o,
+                             const SlotLayout& L, const CellIO& io, const WorkQueue& q, char* gws,
+                             cudaStream_t st) {
+    switch (lc.group) {
+        case 32: return launch_integrate_g<32>(lc, mixed, M, o, L, io, q, gws, st);
+        case 64: return launch_integrate_g<64>(lc, mixed, M, o, L, io, q, gws, st);
+        case 128: return launch_integrate_g<128>(lc, mixed, M, o, L, io, q, gws, st);
+        case 256: return launch_integrate_g<256>(lc, mixed, M, o, L, io, q, gws, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_eval(const LaunchCfg& lc, bool mixed, const DevMech& M, const KOpts& o,
+                        const SlotLayout& L, long long nc, const double* p, const double* T,
+                        const double* rho, const double* Y, double* out, double* J, double* Qdot,
+                        int mode, char* gws, cudaStream_t st) {
+    switch (lc.group) {
+        case 32: return launch_eval_g<32>(lc, mixed, M, o, L, nc, p, T, rho, Y, out, J, Qdot, mode, gws, st);
+        case 64: return launch_eval_g<64>(lc, mixed, M, o, L, nc, p, T, rho, Y, out, J, Qdot, mode, gws, st);
+        case 128: return launch_eval_g<128>(lc, mixed, M, o, L, nc, p, T, rho, Y, out, J, Qdot, mode, gws, st);
+        case 256: return launch_eval_g<256>(lc, mixed, M, o, L, nc, p, T, rho, Y, out, J, Qdot, mode, gws, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t integrate_attributes(int group, bool mixed, int* maxThreads, int* regs) {
+    switch (group) {
+        case 32: return integrate_attributes_g<32>(mixed, maxThreads, regs);
+        case 64: return integrate_attributes_g<64>(mixed, maxThreads, regs);
+        case 128: return integrate_attributes_g<128>(mixed, maxThreads, regs);
+        case 256: return integrate_attributes_g<256>(mixed, maxThreads, regs);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_classify(const CellIO& io, int ns, double Treact, int* order, int* count,
+                            cudaStream_t st) {
+    const int block = 256;
+    long long blocks = (io.nCells + block - 1) / block;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    classify_kernel<<<(int)blocks, block, 0, st>>>(io, ns, Treact, order, count);
+    return cudaGetLastError();
+}
+
+}  // namespace fcs

@@ -1,0 +1,63 @@
+// fcs_launch.h -- kernel launch interface between the C ABI layer and the
+// sm_103a kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include "fcs_internal.h"
+
+namespace fcs {
+
+struct SlotLayout;
+
+// Device views of the per-call cell fields (species-major Y).
+struct CellIO {
+    long long nCells;
+    double deltaT;
+    const double* dtPerCell;   // LTS variant, or null
+    const double* p;
+    const double* rho0;
+    double* T;
+    double* Y;
+    double* subDt;
+    double* RR;                // may be null
+    int* status;               // may be null
+    long long* stats;          // ST_COUNT counters
+    unsigned long long* dtMinBits;  // min of the uncapped sub-steps (positive-double bits)
+};
+
+struct WorkQueue {
+    int* head;                 // next queue index (atomic)
+    const int* order;          // queue position -> cell, or null for identity
+    int n;                     // queue length
+};
+
+struct LaunchCfg {
+    int group;                 // threads per cell: 32, 64, 128, 256
+    int block;                 // threads per block
+    int grid;                  // blocks
+};
+
+cudaError_t launch_integrate(const LaunchCfg& lc, bool mixed, const DevMech& M, const KOpts& o,
+                             const SlotLayout& L, const CellIO& io, const WorkQueue& q, char* gws,
+                             cudaStream_t st);
+cudaError_t launch_eval(const LaunchCfg& lc, bool mixed, const DevMech& M, const KOpts& o,
+                        const SlotLayout& L, long long nc, const double* p, const double* T,
+                        const double* rho, const double* Y, double* out, double* J, double* Qdot,
+                        int mode, char* gws, cudaStream_t st);
+cudaError_t launch_classify(const CellIO& io, int ns, double Treact, int* order, int* count,
+                            cudaStream_t st);
+cudaError_t integrate_attributes(int group, bool mixed, int* maxThreads, int* regs);
+
+// per-group-size instantiations (fcs_kernels_g<G>.cu)
+template<int G>
+cudaError_t launch_integrate_g(const LaunchCfg& lc, bool mixed, const DevMech& M, const KOpts& o,
+                               const SlotLayout& L, const CellIO& io, const WorkQueue& q, char* gws,
+                               cudaStream_t st);
+template<int G>
+cudaError_t launch_eval_g(const LaunchCfg& lc, bool mixed, const DevMech& M, const KOpts& o,
+                          const SlotLayout& L, long long nc, const double* p, const double* T,
+                          const double* rho, const double* Y, double* out, double* J, double* Qdot,
+                          int mode, char* gws, cudaStream_t st);
+template<int G>
+cudaError_t integrate_attributes_g(bool mixed, int* maxThreads, int* regs);
+
+}  // namespace fcs

@@ -1,0 +1,250 @@
+"""ctypes binding of libfcs_cuda.so (the C ABI declared in include/fcs.h).
+
+The product path is the CUDA library only: if ``lib/libfcs_cuda.so`` is
+missing, :func:`load` raises -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from .build import LIB
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+SOLVERS = {"OptRodas34": 0, "OptRosenbrock34": 1, "OptSeulex": 2}
+PRECISIONS = {"fp64": 0, "mixed": 1}
+JACOBIANS = {"exact": 0, "fast": 1}
+PTR_DEVICE = 1
+
+CELL_STATUS = {0: "ok", 1: "max_steps", 2: "nonfinite", 3: "dt_underflow", 4: "skipped"}
+ERRORS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "STATE", 5: "CELLS", 6: "UNSUPPORTED",
+          7: "PARSE"}
+
+EXPORTS = ("fcs_create", "fcs_destroy", "fcs_last_error_string", "fcs_version", "fcs_load_mechanism",
+           "fcs_load_mechanism_foam", "fcs_read_chemistry_properties", "fcs_default_options",
+           "fcs_set_options", "fcs_mechanism_size", "fcs_integrate", "fcs_integrate_lts", "fcs_rhs",
+           "fcs_jacobian", "fcs_rates")
+
+
+class MechDesc(C.Structure):
+    _fields_ = [("n_species", C.c_int32), ("n_reactions", C.c_int32),
+                ("W", _dp), ("T_low", _dp), ("T_high", _dp), ("T_common", _dp),
+                ("high_coeffs", _dp), ("low_coeffs", _dp),
+                ("type", _ip), ("reversible", _ip),
+                ("lhs_offset", _ip), ("lhs_species", _ip),
+                ("rhs_offset", _ip), ("rhs_species", _ip),
+                ("arrhenius", _dp), ("arrhenius2", _dp), ("efficiencies", _dp),
+                ("falloff_params", _dp), ("plog_offset", _ip), ("plog_table", _dp)]
+
+
+class Options(C.Structure):
+    _fields_ = [("solver", C.c_int32), ("jacobian", C.c_int32), ("precision", C.c_int32),
+                ("mapping", C.c_int32), ("abs_tol", C.c_double), ("rel_tol", C.c_double),
+                ("max_steps", C.c_int32), ("max_rejects", C.c_int32), ("T_react", C.c_double),
+                ("delta_t_chem_max", C.c_double)]
+
+
+class StepStats(C.Structure):
+    _fields_ = [("cells_integrated", C.c_int64), ("cells_skipped", C.c_int64),
+                ("cells_failed", C.c_int64), ("attempts", C.c_int64), ("accepted", C.c_int64),
+                ("jacobians", C.c_int64), ("lu_decompositions", C.c_int64),
+                ("rhs_evaluations", C.c_int64), ("linear_solves", C.c_int64),
+                ("kernel_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_LIB: Optional[C.CDLL] = None
+
+
+def load(path: str = LIB) -> C.CDLL:
+    """Load the CUDA library (raises when it has not been built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with fcs.build.build() -- there is no CPU fallback")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.fcs_create.argtypes = [C.POINTER(vp), C.c_int]
+    L.fcs_destroy.argtypes = [vp]
+    L.fcs_last_error_string.argtypes = [vp]
+    L.fcs_last_error_string.restype = C.c_char_p
+    L.fcs_version.restype = C.c_char_p
+    L.fcs_load_mechanism.argtypes = [vp, C.POINTER(MechDesc)]
+    L.fcs_load_mechanism_foam.argtypes = [vp, C.c_char_p, C.c_char_p]
+    L.fcs_read_chemistry_properties.argtypes = [C.c_char_p, C.POINTER(Options), _dp]
+    L.fcs_default_options.argtypes = [C.POINTER(Options)]
+    L.fcs_set_options.argtypes = [vp, C.POINTER(Options)]
+    L.fcs_mechanism_size.argtypes = [vp, _ip, _ip]
+    cell_args = [vp, C.c_int64, C.c_double, vp, vp, vp, vp, vp, vp, vp, C.POINTER(StepStats), _dp, C.c_int32]
+    L.fcs_integrate.argtypes = cell_args
+    L.fcs_integrate_lts.argtypes = [vp, C.c_int64, vp] + cell_args[3:]
+    L.fcs_rhs.argtypes = [vp, C.c_int64, vp, vp, vp, vp, C.c_int32]
+    L.fcs_jacobian.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, C.c_int32]
+    L.fcs_rates.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, vp, C.c_int32]
+    _LIB = L
+    return L
+
+
+class FcsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"fcs error {ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def _addr(a):
+    """Address of a numpy array or a torch tensor (None -> NULL)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()  # torch tensor
+
+
+def make_desc(flat) -> MechDesc:
+    d = MechDesc()
+    keep = []
+
+    def p(a, t):
+        a = np.ascontiguousarray(a)
+        keep.append(a)
+        return a.ctypes.data_as(C.POINTER(t))
+    d.n_species = flat.n_species
+    d.n_reactions = flat.n_reactions
+    d.W = p(flat.W, C.c_double); d.T_low = p(flat.T_low, C.c_double)
+    d.T_high = p(flat.T_high, C.c_double); d.T_common = p(flat.T_common, C.c_double)
+    d.high_coeffs = p(flat.high_coeffs, C.c_double); d.low_coeffs = p(flat.low_coeffs, C.c_double)
+    d.type = p(flat.type, C.c_int32); d.reversible = p(flat.reversible, C.c_int32)
+    d.lhs_offset = p(flat.lhs_offset, C.c_int32); d.lhs_species = p(flat.lhs_species, C.c_int32)
+    d.rhs_offset = p(flat.rhs_offset, C.c_int32); d.rhs_species = p(flat.rhs_species, C.c_int32)
+    d.arrhenius = p(flat.arrhenius, C.c_double); d.arrhenius2 = p(flat.arrhenius2, C.c_double)
+    d.efficiencies = p(flat.efficiencies, C.c_double)
+    d.falloff_params = p(flat.falloff_params, C.c_double)
+    d.plog_offset = p(flat.plog_offset, C.c_int32); d.plog_table = p(flat.plog_table, C.c_double)
+    d._keep = keep
+    return d
+
+
+def read_chemistry_properties(path: str):
+    L = load()
+    o = Options()
+    sub = C.c_double(-1)
+    st = L.fcs_read_chemistry_properties(path.encode(), C.byref(o), C.byref(sub))
+    if st:
+        raise FcsError(st, f"cannot read {path}")
+    return o, sub.value
+
+
+class Context:
+    """One device context (the C ABI's fcs_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.L = load()
+        self.h = C.c_void_p()
+        st = self.L.fcs_create(C.byref(self.h), device)
+        if st:
+            raise FcsError(st, "fcs_create failed")
+        self.ns = None
+        self.options = Options()
+        self.L.fcs_default_options(C.byref(self.options))
+
+    def close(self):
+        if self.h:
+            self.L.fcs_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st:
+            raise FcsError(st, self.L.fcs_last_error_string(self.h).decode())
+
+    def load_mechanism(self, flat):
+        self._desc = make_desc(flat)
+        self._check(self.L.fcs_load_mechanism(self.h, C.byref(self._desc)))
+        self.ns = flat.n_species
+
+    def load_mechanism_foam(self, reactions_path, thermo_path):
+        self._check(self.L.fcs_load_mechanism_foam(self.h, reactions_path.encode(), thermo_path.encode()))
+        ns, nr = C.c_int32(), C.c_int32()
+        self._check(self.L.fcs_mechanism_size(self.h, C.byref(ns), C.byref(nr)))
+        self.ns = ns.value
+        return ns.value, nr.value
+
+    def set_options(self, solver="OptRodas34", jacobian="exact", precision="fp64", mapping=0,
+                    abs_tol=1e-8, rel_tol=1e-4, max_steps=10000, max_rejects=1000, treact=0.0,
+                    dt_chem_max=1e300):
+        o = Options()
+        o.solver = SOLVERS[solver]; o.jacobian = JACOBIANS[jacobian]
+        o.precision = PRECISIONS[precision]; o.mapping = int(mapping)
+        o.abs_tol = abs_tol; o.rel_tol = rel_tol; o.max_steps = max_steps
+        o.max_rejects = max_rejects; o.T_react = treact; o.delta_t_chem_max = dt_chem_max
+        self._check(self.L.fcs_set_options(self.h, C.byref(o)))
+        self.options = o
+
+    def integrate_raw(self, n, dt, p, rho0, T, Y, sub, RR=None, status=None, device=False,
+                      dt_per_cell=None, check=True):
+        """Arrays are numpy (host) or torch CUDA tensors with device=True."""
+        stats = StepStats()
+        dmin = C.c_double(0)
+        flags = PTR_DEVICE if device else 0
+        if dt_per_cell is not None:
+            st = self.L.fcs_integrate_lts(self.h, n, _addr(dt_per_cell), _addr(p), _addr(rho0), _addr(T),
+                                          _addr(Y), _addr(sub), _addr(RR), _addr(status), C.byref(stats),
+                                          C.byref(dmin), flags)
+        else:
+            st = self.L.fcs_integrate(self.h, n, dt, _addr(p), _addr(rho0), _addr(T), _addr(Y), _addr(sub),
+                                      _addr(RR), _addr(status), C.byref(stats), C.byref(dmin), flags)
+        if check and st not in (0, 5):
+            self._check(st)
+        return st, stats.as_dict(), dmin.value
+
+    def integrate(self, cells, dt, dt_per_cell=None):
+        """Integrate a copy of host ``cells``; returns the same dict as the oracle."""
+        n = cells.n
+        T = cells.T.copy()
+        Y = np.ascontiguousarray(cells.Y.copy())
+        sub = cells.subDt.copy()
+        RR = np.zeros_like(Y)
+        status = np.zeros(n, dtype=np.int32)
+        dtc = None if dt_per_cell is None else np.ascontiguousarray(dt_per_cell, dtype=np.float64)
+        st, stats, dmin = self.integrate_raw(n, dt, cells.p, cells.rho0, T, Y, sub, RR, status,
+                                             dt_per_cell=dtc)
+        return dict(T=T, Y=Y, subDt=sub, RR=RR, status=status, deltaTMin=dmin, stats=stats, code=st)
+
+    def rhs(self, p, T, Y):
+        n = T.shape[0]
+        out = np.zeros((self.ns + 1, n))
+        self._check(self.L.fcs_rhs(self.h, n, _addr(np.ascontiguousarray(p)), _addr(np.ascontiguousarray(T)),
+                                   _addr(np.ascontiguousarray(Y)), _addr(out), 0))
+        return out
+
+    def jacobian(self, p, T, Y):
+        n = T.shape[0]
+        N = self.ns + 1
+        J = np.zeros((n, N, N))
+        f = np.zeros((N, n))
+        self._check(self.L.fcs_jacobian(self.h, n, _addr(np.ascontiguousarray(p)),
+                                        _addr(np.ascontiguousarray(T)), _addr(np.ascontiguousarray(Y)),
+                                        _addr(J), _addr(f), 0))
+        return J, f
+
+    def rates(self, p, T, rho, Y):
+        n = T.shape[0]
+        RR = np.zeros((self.ns, n))
+        Q = np.zeros(n)
+        self._check(self.L.fcs_rates(self.h, n, _addr(np.ascontiguousarray(p)), _addr(np.ascontiguousarray(T)),
+                                     _addr(np.ascontiguousarray(rho)), _addr(np.ascontiguousarray(Y)),
+                                     _addr(RR), _addr(Q), 0))
+        return RR, Q

@@ -1,0 +1,249 @@
+/*
+ * fcs.h -- C ABI of the GB300 stiff-chemistry library (libfcs_cuda.so).
+ *
+ * This is the boundary an OpenFOAM-side chemistry model binds to.  It
+ * replaces, for a whole batch of cells at once, the per-cell solver contract
+ * of the FastChemistrySolver plugin:
+ *
+ *   virtual void solve(scalar& p, scalar& T, scalarField& Y, label li,
+ *                      scalar& deltaT, scalar& subDeltaT) const;
+ *       (src/ChemistryModel/FastChemistryModel.H:375-383, implemented by
+ *        src/ODE/OptRodas34/OptRodas34.C:57-121,
+ *        src/ODE/OptRosenbrock34/OptRosenbrock34.C:61-125,
+ *        src/ODE/OptSeulex/OptSeulex.C:103-169)
+ *
+ * together with the cell loop that drives it,
+ *
+ *   scalar FastChemistryModel::solve(const scalar deltaT)
+ *       (src/ChemistryModel/FastChemistryModel_transientSolve.H:2-104)
+ *
+ * and the mechanism loader OptReaction::readInfo
+ *       (src/Reaction/OptReaction.C:348-1339).
+ *
+ * Conventions
+ *   - Every function returns an fcs_status; nothing aborts.  A failure in
+ *     individual cells is reported per cell through cell_status and by the
+ *     FCS_ERR_CELLS return code; the other cells are still written.
+ *   - All arrays are owned by the caller.  Unless FCS_PTR_DEVICE is passed
+ *     they are host pointers and the library copies them to and from its own
+ *     device buffers.  With FCS_PTR_DEVICE they are device pointers on the
+ *     context's GPU and are used in place.
+ *   - Species-major layout: Y[i * n_cells + c] is species i of cell c (one
+ *     contiguous OpenFOAM field per species).
+ *   - One context per host thread; calls on one context are serialised.
+ */
+#ifndef FCS_H
+#define FCS_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fcs_ctx fcs_ctx;
+typedef int32_t fcs_status;
+
+enum {
+    FCS_OK = 0,
+    FCS_ERR_INVALID = 1,      /* bad argument or option                       */
+    FCS_ERR_CUDA = 2,         /* CUDA runtime error (see fcs_last_error_string)*/
+    FCS_ERR_NOMEM = 3,        /* device or host allocation failed             */
+    FCS_ERR_STATE = 4,        /* call out of order (e.g. no mechanism loaded) */
+    FCS_ERR_CELLS = 5,        /* some cells failed; see cell_status           */
+    FCS_ERR_UNSUPPORTED = 6,  /* reaction type or size not supported          */
+    FCS_ERR_PARSE = 7         /* OpenFOAM dictionary could not be read        */
+};
+
+/* Per-cell status codes (cell_status output). */
+enum {
+    FCS_CELL_OK = 0,
+    FCS_CELL_MAX_STEPS = 1,   /* maxSteps exceeded (fatal in the reference, OptRodas34.C:193) */
+    FCS_CELL_NONFINITE = 2,   /* NaN/Inf met in the state or the error norm          */
+    FCS_CELL_DT_UNDERFLOW = 3,/* step size collapsed / too many rejected attempts    */
+    FCS_CELL_SKIPPED = 4      /* T <= Treact: not integrated, RR = 0                  */
+};
+
+/* Reaction kinds of fcs_mechanism_desc.type (OpenFOAM type names without the
+ * reversible/irreversible prefix). */
+enum {
+    FCS_RXN_ARRHENIUS = 0,           /* (ir)reversibleArrhenius                    */
+    FCS_RXN_THIRD_BODY = 1,          /* (ir)reversibleThirdBodyArrhenius           */
+    FCS_RXN_PLOG = 2,                /* (ir)reversibleArrheniusPLOG                */
+    FCS_RXN_LINDEMANN_FALLOFF = 3,   /* (ir)reversibleArrheniusLindemannFallOff    */
+    FCS_RXN_TROE_FALLOFF = 4,        /* (ir)reversibleArrheniusTroeFallOff         */
+    FCS_RXN_SRI_FALLOFF = 5          /* (ir)reversibleArrheniusSRIFallOff          */
+};
+
+enum { FCS_SOLVER_RODAS34 = 0, FCS_SOLVER_ROSENBROCK34 = 1, FCS_SOLVER_SEULEX = 2 };
+enum { FCS_JACOBIAN_EXACT = 0, FCS_JACOBIAN_FAST = 1 };
+/* FCS_PRECISION_MIXED: Jacobian storage and LU in FP32, one FP64-residual
+ * iterative-refinement sweep per linear solve; rates, thermo, equilibrium
+ * constants, state and the step controller stay FP64. */
+enum { FCS_PRECISION_FP64 = 0, FCS_PRECISION_MIXED = 1 };
+/* Cell-to-thread mapping: AUTO lets the autotuner choose. */
+enum { FCS_MAPPING_AUTO = 0, FCS_MAPPING_WARP = 32, FCS_MAPPING_BLOCK64 = 64,
+       FCS_MAPPING_BLOCK128 = 128, FCS_MAPPING_BLOCK256 = 256 };
+
+/* flags for fcs_integrate */
+enum {
+    FCS_PTR_DEVICE = 1,        /* all array arguments are device pointers       */
+    FCS_NO_QUEUE_SORT = 2      /* keep natural cell order in the work queue     */
+};
+
+/*
+ * Mechanism in OpenFOAM file order.  The library reorders the reactions into
+ * the type blocks of OptReaction::readInfo (OptReaction.C:348-1339): constant
+ * Arrhenius (beta == 0 and Ta == 0) first, then the other Arrhenius, then
+ * third-body, fall-off, then PLOG.  Stoichiometric coefficients are expanded
+ * into repeated species entries exactly as readReactionInfo does
+ * (OptReaction.C:29-173).  The host keeps ownership; the library copies.
+ */
+typedef struct fcs_mechanism_desc {
+    int32_t n_species;
+    int32_t n_reactions;
+    const double* W;             /* [Ns] molecular weight, kg/kmol              */
+    const double* T_low;         /* [Ns]                                        */
+    const double* T_high;        /* [Ns]                                        */
+    const double* T_common;      /* [Ns]                                        */
+    const double* high_coeffs;   /* [Ns*7] NASA-7 (janaf) high-T coefficients   */
+    const double* low_coeffs;    /* [Ns*7] NASA-7 low-T coefficients            */
+    const int32_t* type;         /* [R] FCS_RXN_*                               */
+    const int32_t* reversible;   /* [R] 1 = reversible, 0 = irreversible        */
+    const int32_t* lhs_offset;   /* [R+1]                                       */
+    const int32_t* lhs_species;  /* reactant species, repeated by coefficient   */
+    const int32_t* rhs_offset;   /* [R+1]                                       */
+    const int32_t* rhs_species;  /* product species, repeated by coefficient    */
+    const double* arrhenius;     /* [R*3] A, beta, Ta (k0 for fall-off)         */
+    const double* arrhenius2;    /* [R*3] kInf A, beta, Ta for fall-off; may be NULL */
+    const double* efficiencies;  /* [R*Ns] third-body efficiencies (row used for
+                                    third-body and fall-off reactions); may be NULL */
+    const double* falloff_params;/* [R*5] Troe alpha,Ts,Tss,Tsss / SRI a,b,c,d,e */
+    const int32_t* plog_offset;  /* [R+1] rows of plog_table per reaction       */
+    const double* plog_table;    /* [rows*4] p, A, beta, Ta (ArrheniusData)     */
+} fcs_mechanism_desc;
+
+/* chemistryProperties keys: chemistryType{solver}, jacobian, Treact,
+ * initialChemicalTimeStep (used by the caller to seed subDeltaT),
+ * maxChemicalTimeStep, <Solver>Coeffs{absTol, relTol, maxSteps}; plus the
+ * GPU-only keys precision and mapping. */
+typedef struct fcs_options {
+    int32_t solver;              /* FCS_SOLVER_*                      */
+    int32_t jacobian;            /* FCS_JACOBIAN_*                    */
+    int32_t precision;           /* FCS_PRECISION_*                   */
+    int32_t mapping;             /* FCS_MAPPING_*                     */
+    double abs_tol;
+    double rel_tol;
+    int32_t max_steps;           /* default 10000                     */
+    int32_t max_rejects;         /* bound on rejected retries per step (GPU-only, default 64) */
+    double T_react;              /* cells with T <= Treact are skipped */
+    double delta_t_chem_max;     /* maxChemicalTimeStep (default 1e300) */
+} fcs_options;
+
+/* Per-call statistics, summed over cells. */
+typedef struct fcs_step_stats {
+    int64_t cells_integrated;
+    int64_t cells_skipped;
+    int64_t cells_failed;
+    int64_t attempts;            /* attempted steps (accepted + rejected) */
+    int64_t accepted;
+    int64_t jacobians;
+    int64_t lu_decompositions;
+    int64_t rhs_evaluations;
+    int64_t linear_solves;
+    double  kernel_ms;           /* device time of the integration kernel */
+} fcs_step_stats;
+
+fcs_status fcs_create(fcs_ctx** ctx, int device);
+fcs_status fcs_destroy(fcs_ctx* ctx);
+const char* fcs_last_error_string(const fcs_ctx* ctx);
+const char* fcs_version(void);
+
+/* Replaces OptReaction::readInfo (OptReaction.C:348-1339). */
+fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc* desc);
+
+/* Reads an OpenFOAM `reactions` dictionary file and a physicalProperties /
+ * speciesThermo file (species list + per-species specie/thermodynamics
+ * sub-dictionaries) and loads the mechanism, like the plugin constructor
+ * (FastChemistryModel.C:110 -> OptReaction.C:348). */
+fcs_status fcs_load_mechanism_foam(fcs_ctx* ctx, const char* reactions_path,
+                                   const char* thermo_path);
+
+/* Reads the chemistryProperties keys of the plugin (FastChemistryModel.C:45-168,
+ * OptRodas34.C:34-50) into opts: chemistryType{solver}, jacobian, Treact,
+ * <Solver>Coeffs{absTol,relTol,maxSteps}, maxChemicalTimeStep and the optional
+ * FastChemistryGPU{precision, mapping} sub-dictionary.  Unknown keys (balance,
+ * Iter, DLBthreshold, ...) are accepted and ignored.  initial_sub_dt receives
+ * initialChemicalTimeStep (or -1 when absent). */
+fcs_status fcs_read_chemistry_properties(const char* path, fcs_options* opts,
+                                         double* initial_sub_dt);
+
+fcs_status fcs_default_options(fcs_options* opts);
+fcs_status fcs_set_options(fcs_ctx* ctx, const fcs_options* opts);
+
+/* Number of species / reactions of the loaded mechanism. */
+fcs_status fcs_mechanism_size(const fcs_ctx* ctx, int32_t* n_species, int32_t* n_reactions);
+
+/*
+ * Integrate n_cells independent constant-pressure cells over delta_t.
+ * Batched form of FastChemistryModel::solve(deltaT) (transientSolve.H:30-104):
+ *   in:  p[n], rho0[n], T[n], Y[Ns*n], sub_delta_t[n] (deltaTChem_)
+ *   out: T, Y (new state, Y clamped >= 0), sub_delta_t (next initial sub-step,
+ *        capped at maxChemicalTimeStep), RR[Ns*n] = (Y - Y0) * rho0 / delta_t
+ *        (may be NULL), cell_status[n] (may be NULL), stats (may be NULL),
+ *        delta_t_min = min(min over integrated cells of the uncapped
+ *        sub-step, 2*delta_t) (may be NULL).
+ */
+fcs_status fcs_integrate(fcs_ctx* ctx, int64_t n_cells, double delta_t,
+                         const double* p, const double* rho0,
+                         double* T, double* Y, double* sub_delta_t,
+                         double* RR, int32_t* cell_status,
+                         fcs_step_stats* stats, double* delta_t_min,
+                         int32_t flags);
+
+/* Same, with a per-cell delta_t (the local-time-stepping variant
+ * FastChemistryModel::solve(const scalarField& deltaT),
+ * FastChemistryModel_localEulerSolve.H:3-101). */
+fcs_status fcs_integrate_lts(fcs_ctx* ctx, int64_t n_cells, const double* delta_t,
+                             const double* p, const double* rho0,
+                             double* T, double* Y, double* sub_delta_t,
+                             double* RR, int32_t* cell_status,
+                             fcs_step_stats* stats, double* delta_t_min,
+                             int32_t flags);
+
+/*
+ * Right-hand side of the mass-fraction ODE system at each cell state:
+ * dydt[(Ns+1)*n] (species-major, row Ns is dT/dt).  Mirrors
+ * FastChemistryModel::derivatives (FastChemistryModel.C:194-273) on top of
+ * OptReaction::dNdtByV (ReactionRate.C:732-1503).  Y is read-only here (the
+ * in-place max(Y,0) clamp of the reference acts on a copy).
+ */
+fcs_status fcs_rhs(fcs_ctx* ctx, int64_t n_cells, const double* p, const double* T,
+                   const double* Y, double* dydt, int32_t flags);
+
+/*
+ * Analytic Jacobian of the mass-fraction system: J[n][(Ns+1)*(Ns+1)] row-major
+ * per cell, and f = dydt[(Ns+1)*n] species-major.  Mirrors
+ * FastChemistryModel::jacobian (FastChemistryModel.C:489-572) on top of
+ * OptReaction::ddNdtByVdcTp (Jacobian.C:5-1004) and the dC/dY conversion
+ * (Jacobian.C:1943-2059, 2814-2858, 3709-3793, 4541-4568).
+ */
+fcs_status fcs_jacobian(fcs_ctx* ctx, int64_t n_cells, const double* p, const double* T,
+                        const double* Y, double* J, double* dydt, int32_t flags);
+
+/*
+ * Instantaneous source terms (FastChemistryModel::calculate(),
+ * FastChemistryModel.C:715-755): c_i = rho Y_i / W_i (Y not clamped),
+ * RR[i*n+c] = dNdtByV_i * W_i (kg/m^3/s), and the heat release
+ * Qdot[c] = -sum_i Hf_i RR_i with Hf_i the formation enthalpy at 298.15 K
+ * (FastChemistryModel.C:656-685).  Qdot may be NULL.
+ */
+fcs_status fcs_rates(fcs_ctx* ctx, int64_t n_cells, const double* p, const double* T,
+                     const double* rho, const double* Y, double* RR, double* Qdot,
+                     int32_t flags);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FCS_H */

@@ -1,0 +1,1279 @@
+/*
+ * fcs_oracle.c -- CPU restatement of the reference per-cell stiff chemistry
+ * path.  TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and
+ * the cpu_baseline / reference leg of bench.py as the checker; never by the
+ * product library.
+ *
+ * Reference files restated here (paths inside the reference project):
+ *   mechanism ordering    src/Reaction/OptReaction.C:348-1339
+ *   thermo                src/Reaction/ThermoFunctionI.H:1-31, 33-371, 539-636, 799-881
+ *   rates (dNdtByV)       src/Reaction/ReactionRate.C:732-1503, ReactionFunctionI.H:1-721,
+ *                         ChemicalEquilibriumFunctionI.H:14-25
+ *   Jacobian              src/Reaction/Jacobian.C:5-1004, JacobianFunctionI.H (JF11..JF33, JFG)
+ *   dC/dY conversion      src/Reaction/Jacobian.C:2814-2858 (exact), 3709-3741 (T column),
+ *                         3743-3793 (T row), 4541-4568 (fast)
+ *   model closure         src/ChemistryModel/FastChemistryModel.C:194-273, 340-417, 489-572
+ *   LU                    src/LUsolver/LUsolver.C:106-246, 503-660, 3058-3143, 4113-4152
+ *   Rodas34               src/ODE/OptRodas34/OptRodas34.C:57-882, OptRodas34.H:105-149
+ *   Rosenbrock34          src/ODE/OptRosenbrock34/OptRosenbrock34.C:61-678, .H:117-158
+ *   Seulex                src/ODE/OptSeulex/OptSeulex.C:34-734, .H:130-175
+ *   cell loop             src/ChemistryModel/FastChemistryModel_transientSolve.H:30-104
+ */
+#include "fcs_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define RU 8314.470066505449722171761095523834228515625
+#define PSTD 100000.0
+#define KC_CLAMP 1.4901171103413047e-8
+#define KC_CLAMP_G 1.49011611938476E-08
+#define PIV_EPS 2.2204460492503131e-16
+#define SMALL 1.0e-15
+#define VGREAT 1.0e300
+
+struct orc_mech {
+    int ns, n, nr;
+    double *W, *invW, *Tcommon, *coef; /* coef [ns][2][7]: [0] low, [1] high */
+    double TlowMin, ThighMax, TcommonMin, TcommonMax;
+    int nTI, nArr, nTB, nFO, nPlog;
+    /* per reaction, reference order */
+    int *kind, *rev, *fileIdx, *lOff, *lSp, *rOff, *rSp, *tbRow, *plogIdx, *dnu;
+    double *A, *beta, *Ta;
+    double *eff;                 /* [nTB][ns] */
+    int *pOff;                   /* [nPlog+1] */
+    double *pP, *pLogP, *pLogA, *pBeta, *pTa;
+    int maxSp;
+};
+
+int32_t orc_mech_n_species(const orc_mech* m) { return m->ns; }
+
+int32_t orc_mech_order(const orc_mech* m, int32_t* out)
+{
+    for (int i = 0; i < m->nr; i++) out[i] = m->fileIdx[i];
+    return m->nr;
+}
+
+void orc_mech_destroy(orc_mech* m)
+{
+    if (!m) return;
+    free(m->W); free(m->invW); free(m->Tcommon); free(m->coef);
+    free(m->kind); free(m->rev); free(m->fileIdx); free(m->lOff); free(m->lSp);
+    free(m->rOff); free(m->rSp); free(m->tbRow); free(m->plogIdx); free(m->dnu);
+    free(m->A); free(m->beta); free(m->Ta); free(m->eff); free(m->pOff);
+    free(m->pP); free(m->pLogP); free(m->pLogA); free(m->pBeta); free(m->pTa);
+    free(m);
+}
+
+/* Type-block order of OptReaction::readInfo (OptReaction.C:448-1175):
+ * temperature-independent Arrhenius, other Arrhenius, (non-equilibrium),
+ * third-body, fall-off, (chemically activated), PLOG; file order inside each
+ * block. */
+orc_mech* orc_mech_create(const fcs_mechanism_desc* d, int32_t* status)
+{
+    *status = FCS_OK;
+    const int ns = d->n_species, nr = d->n_reactions;
+    for (int r = 0; r < nr; r++) {
+        int t = d->type[r];
+        if (t != FCS_RXN_ARRHENIUS && t != FCS_RXN_THIRD_BODY && t != FCS_RXN_PLOG) {
+            *status = FCS_ERR_UNSUPPORTED;
+            return NULL;
+        }
+    }
+    orc_mech* m = (orc_mech*)calloc(1, sizeof(orc_mech));
+    m->ns = ns; m->n = ns + 1; m->nr = nr;
+    m->W = (double*)malloc(sizeof(double) * ns);
+    m->invW = (double*)malloc(sizeof(double) * ns);
+    m->Tcommon = (double*)malloc(sizeof(double) * ns);
+    m->coef = (double*)malloc(sizeof(double) * ns * 14);
+    m->TlowMin = 1e10; m->ThighMax = 1; m->TcommonMin = 1e10; m->TcommonMax = 0;
+    for (int i = 0; i < ns; i++) {
+        m->W[i] = d->W[i];
+        m->invW[i] = 1.0 / d->W[i];
+        m->Tcommon[i] = d->T_common[i];
+        memcpy(&m->coef[i * 14], &d->low_coeffs[i * 7], 7 * sizeof(double));
+        memcpy(&m->coef[i * 14 + 7], &d->high_coeffs[i * 7], 7 * sizeof(double));
+        if (m->TlowMin > d->T_low[i]) m->TlowMin = d->T_low[i];
+        if (m->ThighMax < d->T_high[i]) m->ThighMax = d->T_high[i];
+        if (d->T_common[i] > m->TcommonMax) m->TcommonMax = d->T_common[i];
+        if (d->T_common[i] < m->TcommonMin) m->TcommonMin = d->T_common[i];
+    }
+    int* order = (int*)malloc(sizeof(int) * (nr > 0 ? nr : 1));
+    int k = 0;
+    for (int pass = 0; pass < 4; pass++) {
+        for (int r = 0; r < nr; r++) {
+            int t = d->type[r];
+            double beta = d->arrhenius[3 * r + 1], Ta = d->arrhenius[3 * r + 2];
+            int tind = (beta == 0 && Ta == 0);
+            if ((pass == 0 && t == FCS_RXN_ARRHENIUS && tind) ||
+                (pass == 1 && t == FCS_RXN_ARRHENIUS && !tind) ||
+                (pass == 2 && t == FCS_RXN_THIRD_BODY) ||
+                (pass == 3 && t == FCS_RXN_PLOG))
+                order[k++] = r;
+        }
+    }
+#define ALLOC_I(x, n) x = (int*)calloc((n) > 0 ? (n) : 1, sizeof(int))
+#define ALLOC_D(x, n) x = (double*)calloc((n) > 0 ? (n) : 1, sizeof(double))
+    ALLOC_I(m->kind, nr); ALLOC_I(m->rev, nr); ALLOC_I(m->fileIdx, nr);
+    ALLOC_I(m->lOff, nr + 1); ALLOC_I(m->rOff, nr + 1); ALLOC_I(m->tbRow, nr);
+    ALLOC_I(m->plogIdx, nr); ALLOC_I(m->dnu, nr);
+    ALLOC_D(m->A, nr); ALLOC_D(m->beta, nr); ALLOC_D(m->Ta, nr);
+    int nl_tot = d->lhs_offset[nr], nr_tot = d->rhs_offset[nr];
+    ALLOC_I(m->lSp, nl_tot); ALLOC_I(m->rSp, nr_tot);
+    int nTB = 0, nPlog = 0, plogRows = 0;
+    for (int r = 0; r < nr; r++) {
+        if (d->type[r] == FCS_RXN_THIRD_BODY) nTB++;
+        if (d->type[r] == FCS_RXN_PLOG) { nPlog++; plogRows += d->plog_offset[r + 1] - d->plog_offset[r]; }
+    }
+    m->nTB = nTB; m->nPlog = nPlog;
+    ALLOC_D(m->eff, nTB * ns);
+    ALLOC_I(m->pOff, nPlog + 1);
+    ALLOC_D(m->pP, plogRows); ALLOC_D(m->pLogP, plogRows); ALLOC_D(m->pLogA, plogRows);
+    ALLOC_D(m->pBeta, plogRows); ALLOC_D(m->pTa, plogRows);
+    int lo = 0, ro = 0, tb = 0, pl = 0, prow = 0;
+    m->maxSp = 0;
+    for (int i = 0; i < nr; i++) {
+        int r = order[i];
+        m->fileIdx[i] = r;
+        m->kind[i] = d->type[r];
+        m->rev[i] = d->reversible[r] ? 1 : 0;
+        m->A[i] = d->arrhenius[3 * r + 0];
+        m->beta[i] = d->arrhenius[3 * r + 1];
+        m->Ta[i] = d->arrhenius[3 * r + 2];
+        m->lOff[i] = lo;
+        for (int j = d->lhs_offset[r]; j < d->lhs_offset[r + 1]; j++) m->lSp[lo++] = d->lhs_species[j];
+        m->rOff[i] = ro;
+        for (int j = d->rhs_offset[r]; j < d->rhs_offset[r + 1]; j++) m->rSp[ro++] = d->rhs_species[j];
+        int nlr = d->lhs_offset[r + 1] - d->lhs_offset[r];
+        int nrr = d->rhs_offset[r + 1] - d->rhs_offset[r];
+        if (nlr > m->maxSp) m->maxSp = nlr;
+        if (nrr > m->maxSp) m->maxSp = nrr;
+        m->dnu[i] = nrr - nlr;
+        m->tbRow[i] = -1;
+        m->plogIdx[i] = -1;
+        if (m->kind[i] == FCS_RXN_THIRD_BODY) {
+            for (int s = 0; s < ns; s++) m->eff[tb * ns + s] = d->efficiencies[(size_t)r * ns + s];
+            m->tbRow[i] = tb++;
+        }
+        if (m->kind[i] == FCS_RXN_PLOG) {
+            m->plogIdx[i] = pl;
+            m->pOff[pl] = prow;
+            for (int q = d->plog_offset[r]; q < d->plog_offset[r + 1]; q++) {
+                const double* row = &d->plog_table[4 * q];
+                m->pP[prow] = row[0];
+                m->pLogP[prow] = log(row[0]);
+                m->pLogA[prow] = log(row[1]);
+                m->pBeta[prow] = row[2];
+                m->pTa[prow] = row[3];
+                prow++;
+            }
+            pl++;
+        }
+        if (m->kind[i] == FCS_RXN_ARRHENIUS) {
+            m->nArr++;
+            if (m->beta[i] == 0 && m->Ta[i] == 0) m->nTI++;
+        }
+    }
+    m->pOff[pl] = prow;
+    m->lOff[nr] = lo; m->rOff[nr] = ro;
+    free(order);
+    return m;
+}
+
+/* ------------------------------------------------------------------------ */
+/* per-thread workspace                                                      */
+
+typedef struct {
+    const orc_mech* m;
+    int n;
+    double *C, *B, *dBdT, *Cp, *Ha, *dCpdT, *rhoMvj, *WiByrhoM;
+    double *Kf, *dKfdT, *M, *Kplog, *dKplog;
+    double *Jc, *Jy, *a;       /* N*N each */
+    double *vec[16];           /* N each */
+    int *piv;
+    double *invD;
+    double *table;             /* Seulex: 12*N */
+    double rhoM;               /* last thermo rhoM (kg/m3) */
+    double invT;
+    int64_t cnt[ORC_NCOUNTERS];
+} ws_t;
+
+static ws_t* ws_create(const orc_mech* m)
+{
+    ws_t* w = (ws_t*)calloc(1, sizeof(ws_t));
+    int n = m->n, ns = m->ns, nr = m->nr;
+    w->m = m; w->n = n;
+    w->C = (double*)calloc(ns, sizeof(double));
+    w->B = (double*)calloc(ns, sizeof(double));
+    w->dBdT = (double*)calloc(ns, sizeof(double));
+    w->Cp = (double*)calloc(ns, sizeof(double));
+    w->Ha = (double*)calloc(ns, sizeof(double));
+    w->dCpdT = (double*)calloc(ns, sizeof(double));
+    w->rhoMvj = (double*)calloc(ns, sizeof(double));
+    w->WiByrhoM = (double*)calloc(ns, sizeof(double));
+    w->Kf = (double*)calloc(nr + 1, sizeof(double));
+    w->dKfdT = (double*)calloc(nr + 1, sizeof(double));
+    w->M = (double*)calloc(m->nTB + 1, sizeof(double));
+    w->Kplog = (double*)calloc(m->nPlog + 1, sizeof(double));
+    w->dKplog = (double*)calloc(m->nPlog + 1, sizeof(double));
+    w->Jc = (double*)calloc((size_t)n * n, sizeof(double));
+    w->Jy = (double*)calloc((size_t)n * n, sizeof(double));
+    w->a = (double*)calloc((size_t)n * n, sizeof(double));
+    for (int i = 0; i < 16; i++) w->vec[i] = (double*)calloc(n, sizeof(double));
+    w->piv = (int*)calloc(n, sizeof(int));
+    w->invD = (double*)calloc(n, sizeof(double));
+    w->table = (double*)calloc((size_t)12 * n, sizeof(double));
+    return w;
+}
+
+static void ws_destroy(ws_t* w)
+{
+    free(w->C); free(w->B); free(w->dBdT); free(w->Cp); free(w->Ha); free(w->dCpdT);
+    free(w->rhoMvj); free(w->WiByrhoM); free(w->Kf); free(w->dKfdT); free(w->M);
+    free(w->Kplog); free(w->dKplog); free(w->Jc); free(w->Jy); free(w->a);
+    for (int i = 0; i < 16; i++) free(w->vec[i]);
+    free(w->piv); free(w->invD); free(w->table);
+    free(w);
+}
+
+/* ------------------------------------------------------------------------ */
+/* thermo: ThermoFunctionI.H                                                 */
+
+static inline const double* coeffs(const orc_mech* m, int i, double Tbranch)
+{
+    /* setPtrCoeffs (ThermoFunctionI.H:1-31) */
+    if (Tbranch < m->TcommonMin) return &m->coef[i * 14];
+    if (Tbranch > m->TcommonMax) return &m->coef[i * 14 + 7];
+    return (Tbranch < m->Tcommon[i]) ? &m->coef[i * 14] : &m->coef[i * 14 + 7];
+}
+
+/* exponent of exp(-G/RT) (ThermoFunctionI.H:539-636): B = a0(lnT-1) + a1 T/2 +
+ * a2 T^2/6 + a3 T^3/12 + a4 T^4/20 - a5/T + a6 */
+static inline double gibbs_exponent(const double* a, double T, double invT, double logT)
+{
+    double v = fma(a[4] * 0.05, T, a[3] * (1.0 / 12.0));
+    v = fma(v, T, a[2] * (1.0 / 6.0));
+    v = fma(v, T, a[1] * 0.5);
+    v = fma(v, T, -(a[5] * invT));
+    v = v + a[6];
+    return fma(a[0], logT - 1.0, v);
+}
+
+static inline double cp_of(const double* a, double T, double RuInvW)
+{
+    double v = fma(a[4], T, a[3]);
+    v = fma(v, T, a[2]);
+    v = fma(v, T, a[1]);
+    v = fma(v, T, a[0]);
+    return RuInvW * v;
+}
+
+static inline double ha_of(const double* a, double T, double RuInvW)
+{
+    double v = fma(a[4], T * 0.2, a[3] * 0.25);
+    v = fma(v, T, a[2] * (1.0 / 3.0));
+    v = fma(v, T, a[1] * 0.5);
+    v = fma(v, T, a[0]);
+    v = fma(v, T, a[5]);
+    return RuInvW * v;
+}
+
+/* ------------------------------------------------------------------------ */
+/* rate constants shared by RHS and Jacobian                                 */
+
+static void plog_rates(const orc_mech* m, ws_t* w, double p, double logT, double invT, int withDeriv)
+{
+    /* ReactionRate.C:577-727 / Jacobian.C:798-1000 (uniformPressureRange false) */
+    const double logP = log(p);
+    for (int i = 0; i < m->nPlog; i++) {
+        const int o = m->pOff[i], len = m->pOff[i + 1] - o;
+        double lk, dk;
+        if (p <= m->pP[o]) {
+            lk = m->pLogA[o] + m->pBeta[o] * logT - m->pTa[o] * invT;
+            dk = (m->pBeta[o] + m->pTa[o] * invT) * invT;
+        } else if (p >= m->pP[o + len - 1]) {
+            const int e = o + len - 1;
+            lk = m->pLogA[e] + m->pBeta[e] * logT - m->pTa[e] * invT;
+            dk = (m->pBeta[e] + m->pTa[e] * invT) * invT;
+        } else {
+            int idx = 0;
+            for (int j = 0; j < len - 1; j++) {
+                if (m->pP[o + j] <= p && p <= m->pP[o + j + 1]) { idx = j; break; }
+            }
+            const int a = o + idx, b = a + 1;
+            const double fr = (logP - m->pLogP[a]) / (m->pLogP[b] - m->pLogP[a]);
+            lk = m->pLogA[a] + m->pBeta[a] * logT - m->pTa[a] * invT
+               + ((m->pLogA[b] - m->pLogA[a]) + (m->pBeta[b] - m->pBeta[a]) * logT
+                  - (m->pTa[b] - m->pTa[a]) * invT) * fr;
+            dk = invT * (m->pBeta[a] + m->pTa[a] * invT
+                         + (m->pBeta[b] - m->pBeta[a] + (m->pTa[b] - m->pTa[a]) * invT) * fr);
+        }
+        const double k = exp(lk);
+        w->Kplog[i] = k;
+        if (withDeriv) w->dKplog[i] = k * dk;
+    }
+}
+
+static void arrhenius_rates(const orc_mech* m, ws_t* w, double logT, double invT, int withDeriv)
+{
+    /* ReactionRate.C:79-130 (Kf) and Jacobian.C:108-175 (dKf/dT) */
+    for (int i = 0; i < m->nr; i++) {
+        if (m->kind[i] == FCS_RXN_PLOG) continue;
+        if (i < m->nTI) { w->Kf[i] = m->A[i]; w->dKfdT[i] = 0; continue; }
+        const double k = m->A[i] * exp(fma(m->beta[i], logT, -(m->Ta[i] * invT)));
+        w->Kf[i] = k;
+        if (withDeriv) w->dKfdT[i] = k * (fma(m->Ta[i], invT, m->beta[i]) * invT);
+    }
+}
+
+static void third_body(const orc_mech* m, ws_t* w)
+{
+    /* M = E.C (ReactionRate.C:131-354) */
+    for (int t = 0; t < m->nTB; t++) {
+        double s = 0;
+        const double* e = &m->eff[(size_t)t * m->ns];
+        for (int j = 0; j < m->ns; j++) s += e[j] * w->C[j];
+        w->M[t] = s;
+    }
+}
+
+static inline double prod_sp(const int* sp, int n, const double* C)
+{
+    double v = 1.0;
+    for (int q = 0; q < n; q++) v *= C[sp[q]];
+    return v;
+}
+
+/* Kc = Kp (Pstd/(Ru T))^dnu, clamped from below (ReactionFunctionI.H RF11..RF33,
+ * ChemicalEquilibriumFunctionI.H:14-25) */
+static inline double equilibrium(const orc_mech* m, int i, const double* E, double PByRT)
+{
+    const int* L = &m->lSp[m->lOff[i]];
+    const int* R = &m->rSp[m->rOff[i]];
+    const int nl = m->lOff[i + 1] - m->lOff[i], nr = m->rOff[i + 1] - m->rOff[i];
+    double num = 1.0, den = 1.0;
+    for (int q = 0; q < nr; q++) num *= E[R[q]];
+    for (int q = 0; q < nl; q++) den *= E[L[q]];
+    double Kc = num / den;
+    const int dnu = m->dnu[i];
+    if (dnu != 0) {
+        /* update_Pow_pByRT_SumVki2 table (ChemicalEquilibriumFunctionI.H:14-25);
+         * fastPow for the general form (OptReaction.H:1405-1420) */
+        double f;
+        if (dnu == -2) f = 1 / (PByRT * PByRT);
+        else if (dnu == -1) f = 1 / PByRT;
+        else if (dnu == 1) f = PByRT;
+        else if (dnu == 2) f = PByRT * PByRT;
+        else {
+            double xx = dnu < 0 ? 1 / PByRT : PByRT;
+            f = 1;
+            for (int q = dnu; q != 0; q /= 2) { if (q % 2) f *= xx; xx *= xx; }
+        }
+        Kc = Kc * f;
+    }
+    const double clamp = (nl > 3 || nr > 3) ? KC_CLAMP_G : KC_CLAMP;
+    return Kc > clamp ? Kc : clamp;
+}
+
+/* ------------------------------------------------------------------------ */
+/* dNdtByV: ReactionRate.C:732-1503                                          */
+
+static void dNdtByV(const orc_mech* m, ws_t* w, double p, double T, double* omega,
+                    double* Cp, double* Ha, double TforCpHa, int cpha)
+{
+    const int ns = m->ns;
+    double Tc = T < m->TlowMin ? m->TlowMin : T;
+    Tc = Tc > m->ThighMax ? m->ThighMax : Tc;
+    const double logT = log(Tc), invT = 1.0 / Tc;
+    for (int i = 0; i < ns; i++) {
+        const double* a = coeffs(m, i, Tc);
+        w->B[i] = exp(gibbs_exponent(a, Tc, invT, logT));
+        if (cpha) {
+            const double RuInvW = m->invW[i] * RU;
+            const double Tp = cpha == 1 ? Tc : TforCpHa;
+            Cp[i] = cp_of(a, Tp, RuInvW);
+            Ha[i] = ha_of(a, Tp, RuInvW);
+        }
+    }
+    const double PByRT = PSTD / (RU * Tc);
+    arrhenius_rates(m, w, logT, invT, 0);
+    third_body(m, w);
+    for (int i = 0; i < m->nr; i++)
+        if (m->kind[i] == FCS_RXN_THIRD_BODY) w->Kf[i] *= w->M[m->tbRow[i]];
+    if (m->nPlog) plog_rates(m, w, p, logT, invT, 0);
+    memset(omega, 0, sizeof(double) * ns);
+    for (int i = 0; i < m->nr; i++) {
+        const double Kf = (m->kind[i] == FCS_RXN_PLOG) ? w->Kplog[m->plogIdx[i]] : w->Kf[i];
+        const int* L = &m->lSp[m->lOff[i]];
+        const int* R = &m->rSp[m->rOff[i]];
+        const int nl = m->lOff[i + 1] - m->lOff[i], nr = m->rOff[i + 1] - m->rOff[i];
+        double Kr = 0;
+        if (m->rev[i]) Kr = Kf / equilibrium(m, i, w->B, PByRT);
+        const double q = Kf * prod_sp(L, nl, w->C) - Kr * prod_sp(R, nr, w->C);
+        for (int s = 0; s < nl; s++) omega[L[s]] -= q;
+        for (int s = 0; s < nr; s++) omega[R[s]] += q;
+    }
+}
+
+/* FastChemistryModel::derivatives, 7-arg (cpha=1: Cp/Ha at the clamped T,
+ * FastChemistryModel.C:194-273) and 6-arg (cpha=2: Cp/Ha from CpHa(T) at the
+ * unclamped T, FastChemistryModel.C:340-417).  Clamps Y >= 0 in place. */
+static void derivatives(const orc_mech* m, ws_t* w, double p, double* YT, double* dYTdt, int cpha)
+{
+    const int ns = m->ns;
+    const double T = YT[ns];
+    for (int i = 0; i < ns; i++) YT[i] = YT[i] > 0 ? YT[i] : 0;
+    const double RuTByP = RU * T / p;
+    double sum = 0;
+    for (int i = 0; i < ns; i++) sum = fma(YT[i] * m->invW[i], RuTByP, sum);
+    const double invrhoM = sum;
+    const double rhoM = 1.0 / sum;
+    for (int i = 0; i < ns; i++) w->C[i] = rhoM * m->invW[i] * YT[i];
+    double* Cp = w->Cp;
+    double* Ha = w->Ha;
+    dNdtByV(m, w, p, T, dYTdt, Cp, Ha, T, cpha);
+    double CpM = 0, dTdt = 0;
+    for (int i = 0; i < ns; i++) {
+        dYTdt[i] = (m->W[i] * invrhoM) * dYTdt[i];
+        CpM = fma(YT[i], Cp[i], CpM);
+        dTdt = fma(Ha[i], dYTdt[i], dTdt);
+    }
+    dYTdt[ns] = -dTdt / CpM;
+    w->cnt[ORC_RHS]++;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Jacobian: Jacobian.C:5-1004 + JF11..JF33/JFG + conversion                 */
+
+static void jacobian(const orc_mech* m, ws_t* w, const orc_options* o, double p,
+                     double* YT, double* dYTdt, double* J)
+{
+    const int ns = m->ns, n = m->n;
+    for (int i = 0; i < ns; i++) YT[i] = YT[i] > 0 ? YT[i] : 0;
+    const double Traw = YT[ns];
+    double Tc = Traw < m->TlowMin ? m->TlowMin : Traw;
+    Tc = Tc > m->ThighMax ? m->ThighMax : Tc;
+    const double logT = log(Tc), invT = 1.0 / Tc;
+    double* Jc = w->Jc;
+    memset(Jc, 0, sizeof(double) * n * n);
+    memset(dYTdt, 0, sizeof(double) * n);
+
+    /* JacobianThermo (ThermoFunctionI.H:33-371), evaluated at the clamped T */
+    const double RuTByP = (RU * Tc) / p;
+    double rs = 0, MWs = 0;
+    for (int i = 0; i < ns; i++) {
+        const double* a = coeffs(m, i, Tc);
+        rs = fma(RuTByP, YT[i] * m->invW[i], rs);
+        MWs = fma(YT[i], m->invW[i], MWs);
+        w->dBdT[i] = fma(fma(a[5], invT, a[0]), invT,
+                         fma(fma(fma(a[4] * 0.2, Tc, a[3] * 0.25), Tc, a[2] * (1.0 / 3.0)), Tc, a[1] * 0.5));
+        w->B[i] = exp(gibbs_exponent(a, Tc, invT, logT));
+        const double RuInvW = m->invW[i] * RU;
+        w->dCpdT[i] = RuInvW * fma(Tc, fma(Tc, fma(Tc, 4 * a[4], 3 * a[3]), 2 * a[2]), a[1]);
+        w->Cp[i] = cp_of(a, Tc, RuInvW);
+        w->Ha[i] = ha_of(a, Tc, RuInvW);
+    }
+    const double MW = 1.0 / MWs;
+    const double invRhoM = rs;
+    const double rhoM = 1.0 / rs;
+    w->rhoM = rhoM;
+    w->invT = invT;
+    double CpM = 0, dCpMdT = 0;
+    for (int i = 0; i < ns; i++) {
+        w->rhoMvj[i] = MW * m->invW[i];
+        w->WiByrhoM[i] = invRhoM * m->W[i];
+        w->C[i] = rhoM * YT[i] * m->invW[i];
+        CpM = fma(YT[i], w->Cp[i], CpM);
+        dCpMdT = fma(YT[i], w->dCpdT[i], dCpMdT);
+    }
+    const double PByRT = PSTD / (RU * Tc);
+    arrhenius_rates(m, w, logT, invT, 1);
+    third_body(m, w);
+    if (m->nPlog) plog_rates(m, w, p, logT, invT, 1);
+    const double* C = w->C;
+    double* omega = dYTdt;
+    for (int i = 0; i < m->nr; i++) {
+        double Kf, dKfdT, dKfdC = 0;
+        int tb = m->tbRow[i];
+        if (m->kind[i] == FCS_RXN_PLOG) { Kf = w->Kplog[m->plogIdx[i]]; dKfdT = w->dKplog[m->plogIdx[i]]; }
+        else { Kf = w->Kf[i]; dKfdT = w->dKfdT[i]; }
+        if (tb >= 0) {
+            /* Jacobian.C:401-420: dKf/dM = Kf(before M), Kf *= M, dKf/dT *= M */
+            dKfdC = Kf;
+            Kf *= w->M[tb];
+            dKfdT *= w->M[tb];
+        }
+        const int* L = &m->lSp[m->lOff[i]];
+        const int* R = &m->rSp[m->rOff[i]];
+        const int nl = m->lOff[i + 1] - m->lOff[i], nr = m->rOff[i + 1] - m->rOff[i];
+        double Kr = 0, dKrdT = 0, invKc = 0;
+        if (m->rev[i]) {
+            /* JF* reversible branch, e.g. JacobianFunctionI.H:1127-1297 */
+            const double Kc = equilibrium(m, i, w->B, PByRT);
+            const double clamp = (nl > 3 || nr > 3) ? KC_CLAMP_G : KC_CLAMP;
+            double sumV = 0;
+            for (int q = 0; q < nr; q++) sumV += w->dBdT[R[q]];
+            double sumL = 0;
+            for (int q = 0; q < nl; q++) sumL += w->dBdT[L[q]];
+            sumV -= sumL;
+            const double dKcdTByKc = sumV - m->dnu[i] * invT;
+            invKc = 1.0 / Kc;
+            Kr = Kf * invKc;
+            dKrdT = dKfdT * invKc - (Kc > clamp ? Kr * dKcdTByKc : 0);
+            for (int pp = 0; pp < nr; pp++) {
+                double d = 1.0;
+                for (int q = 0; q < nr; q++) if (q != pp) d *= C[R[q]];
+                const double v = -Kr * d;
+                const int col = R[pp];
+                for (int s = 0; s < nl; s++) Jc[L[s] * n + col] -= v;
+                for (int s = 0; s < nr; s++) Jc[R[s] * n + col] += v;
+            }
+        }
+        const double CF = prod_sp(L, nl, C);
+        const double CR = prod_sp(R, nr, C);
+        const double q = Kf * CF - Kr * CR;
+        for (int s = 0; s < nl; s++) omega[L[s]] -= q;
+        for (int s = 0; s < nr; s++) omega[R[s]] += q;
+        const double dqdT = dKfdT * CF - dKrdT * CR;
+        for (int s = 0; s < nl; s++) Jc[L[s] * n + ns] -= dqdT;
+        for (int s = 0; s < nr; s++) Jc[R[s] * n + ns] += dqdT;
+        for (int pp = 0; pp < nl; pp++) {
+            double d = 1.0;
+            for (int qq = 0; qq < nl; qq++) if (qq != pp) d *= C[L[qq]];
+            const double v = Kf * d;
+            const int col = L[pp];
+            for (int s = 0; s < nl; s++) Jc[L[s] * n + col] -= v;
+            for (int s = 0; s < nr; s++) Jc[R[s] * n + col] += v;
+        }
+        if (tb >= 0) {
+            const double dKrdC = dKfdC * invKc;
+            const double* e = &m->eff[(size_t)tb * ns];
+            for (int j = 0; j < ns; j++) {
+                const double Wd = (dKfdC * e[j]) * CF - (dKrdC * e[j]) * CR;
+                for (int s = 0; s < nl; s++) Jc[L[s] * n + j] -= Wd;
+                for (int s = 0; s < nr; s++) Jc[R[s] * n + j] += Wd;
+            }
+        }
+    }
+
+    /* dC/dY conversion */
+    double* dYdt_m = w->vec[15];
+    for (int i = 0; i < ns; i++) dYdt_m[i] = omega[i] * w->WiByrhoM[i];
+    if (o->jacobian == FCS_JACOBIAN_FAST) {
+        /* FastddYdtdY (Jacobian.C:4541-4568) */
+        for (int i = 0; i < ns; i++)
+            for (int j = 0; j < ns; j++)
+                J[i * n + j] = w->WiByrhoM[i] * (Jc[i * n + j] * (rhoM * m->invW[j]))
+                             + w->rhoMvj[j] * dYdt_m[i];
+    } else if (o->conversion_as_written) {
+        /* ddYdtdY (Jacobian.C:2814-2858), O(N^3) as written */
+        double* arr = w->vec[14];
+        for (int j = 0; j < ns; j++) {
+            for (int i = 0; i < ns; i++)
+                arr[i] = (rhoM * m->invW[i]) * ((i == j ? 1.0 : 0.0) - w->rhoMvj[j] * YT[i]);
+            for (int i = 0; i < ns; i++) {
+                double s = 0;
+                for (int k = 0; k < ns; k++) s += Jc[i * n + k] * arr[k];
+                J[i * n + j] = w->WiByrhoM[i] * s + w->rhoMvj[j] * dYdt_m[i];
+            }
+        }
+    } else {
+        /* the same conversion as diag scaling + rank-1:
+         * sum_k Jc_ik (rho/W_k)(delta_kj - m_j Y_k) = Jc_ij rho/W_j - m_j sum_k Jc_ik C_k */
+        for (int i = 0; i < ns; i++) {
+            double S = 0;
+            for (int k = 0; k < ns; k++) S = fma(Jc[i * n + k], C[k], S);
+            for (int j = 0; j < ns; j++)
+                J[i * n + j] = w->WiByrhoM[i] * fma(Jc[i * n + j], rhoM * m->invW[j], -(w->rhoMvj[j] * S))
+                             + w->rhoMvj[j] * dYdt_m[i];
+        }
+    }
+    /* T column, ddYdtdTP (Jacobian.C:3709-3741) */
+    for (int i = 0; i < ns; i++) {
+        double v = Jc[i * n + ns];
+        for (int j = 0; j < ns; j++) v -= Jc[i * n + j] * C[j] * invT;
+        J[i * n + ns] = w->WiByrhoM[i] * v + invT * dYdt_m[i];
+        dYTdt[i] = dYdt_m[i];
+    }
+    /* T row, ddTdtdYT (Jacobian.C:3743-3793) */
+    double dTdt = 0;
+    for (int i = 0; i < ns; i++) dTdt -= dYTdt[i] * w->Ha[i];
+    dTdt /= CpM;
+    dYTdt[ns] = dTdt;
+    double dd = 0;
+    for (int i = 0; i < ns; i++) {
+        double v = 0;
+        for (int j = 0; j < ns; j++) v -= J[j * n + i] * w->Ha[j];
+        v -= w->Cp[i] * dTdt;
+        J[ns * n + i] = v / CpM;
+        dd -= dYTdt[i] * w->Cp[i] + J[i * n + ns] * w->Ha[i];
+    }
+    dd -= dTdt * dCpMdT;
+    J[ns * n + ns] = dd / CpM;
+    w->cnt[ORC_JAC]++;
+}
+
+/* ------------------------------------------------------------------------ */
+/* LU with 4-row-panel pivoting: LUsolver.C:106-246 (panel), 503-660 (2- and
+ * 3-row tails), 3058-3143 (driver); solve LUsolver.C:3145-3171, 4113-4152.   */
+
+static inline void swap_rows(double* a, int n, int r0, int r1)
+{
+    double* x = &a[(size_t)r0 * n];
+    double* y = &a[(size_t)r1 * n];
+    for (int j = 0; j < n; j++) { double t = x[j]; x[j] = y[j]; y[j] = t; }
+}
+
+/* pivot row for column k at position pos of a panel holding `size` rows */
+static int choose_pivot(const double* a, int n, int k, int pos, int size)
+{
+    const int cand = size - pos;
+    if (cand <= 1) return k;
+    if (size == 4 && pos == 0) {
+        int best = 0; double t = 0;
+        for (int c = 0; c < 4; c++) if (t < fabs(a[(size_t)(k + c) * n + k])) { best = c; t = fabs(a[(size_t)(k + c) * n + k]); }
+        return k + best;
+    }
+    if (size == 4 && pos == 1) {
+        /* LUsolver.C:169-185: note temp keeps the signed value of row 2 */
+        double t = fabs(a[(size_t)k * n + k]); int best = 0;
+        if (t < fabs(a[(size_t)(k + 1) * n + k])) { best = 1; t = a[(size_t)(k + 1) * n + k]; }
+        if (t < fabs(a[(size_t)(k + 2) * n + k])) { best = 2; }
+        return k + best;
+    }
+    if (size == 3 && pos == 0) {
+        int best = 0; double t = 0;
+        for (int c = 0; c < 3; c++) if (t < fabs(a[(size_t)(k + c) * n + k])) { best = c; t = fabs(a[(size_t)(k + c) * n + k]); }
+        return k + best;
+    }
+    /* two candidates: swap if |a_kk| < |a_k+1,k| */
+    return (fabs(a[(size_t)k * n + k]) < fabs(a[(size_t)(k + 1) * n + k])) ? k + 1 : k;
+}
+
+static void lu_decompose(double* a, int n, int* piv, double* invD)
+{
+    const int rem = n % 4;
+    for (int i = 0; i < n; i++) piv[i] = i;
+    for (int k = 0; k < n; k++) {
+        const int k0 = (k < n - rem) ? (k & ~3) : n - rem;
+        const int size = (k < n - rem) ? 4 : rem;
+        const int pos = k - k0;
+        if (size == 1) {
+            invD[k] = 1.0 / a[(size_t)k * n + k];
+            continue;
+        }
+        const int p = choose_pivot(a, n, k, pos, size);
+        if (p != k) { swap_rows(a, n, k, p); piv[k] = p; }
+        if (a[(size_t)k * n + k] == 0) a[(size_t)k * n + k] = PIV_EPS;
+        const double rinv = 1.0 / a[(size_t)k * n + k];
+        invD[k] = rinv;
+        for (int i = k + 1; i < n; i++) {
+            const double l = a[(size_t)i * n + k] * rinv;
+            a[(size_t)i * n + k] = l;
+            if (l == 0) continue;
+            double* ri = &a[(size_t)i * n];
+            const double* rk = &a[(size_t)k * n];
+            for (int j = k + 1; j < n; j++) ri[j] = fma(-l, rk[j], ri[j]);
+        }
+    }
+}
+
+static void lu_solve(const double* a, int n, const int* piv, const double* invD, double* b)
+{
+    for (int j = 0; j < n; j++) {
+        if (piv[j] != j) { double t = b[piv[j]]; b[piv[j]] = b[j]; b[j] = t; }
+    }
+    for (int i = 1; i < n; i++) {
+        double s = b[i];
+        const double* ri = &a[(size_t)i * n];
+        for (int j = 0; j < i; j++) s = fma(-ri[j], b[j], s);
+        b[i] = s;
+    }
+    for (int i = n - 1; i >= 0; i--) {
+        double s = b[i];
+        const double* ri = &a[(size_t)i * n];
+        for (int j = i + 1; j < n; j++) s = fma(-ri[j], b[j], s);
+        b[i] = s * invD[i];
+    }
+}
+
+int32_t orc_lu_solve(int32_t n, double* a, int32_t nrhs, double* b, int32_t* piv, double* invD)
+{
+    lu_decompose(a, n, piv, invD);
+    for (int r = 0; r < nrhs; r++) lu_solve(a, n, piv, invD, &b[(size_t)r * n]);
+    return FCS_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Rosenbrock methods                                                        */
+
+typedef struct {
+    const orc_mech* m; ws_t* w; const orc_options* o; double p;
+} cellctx;
+
+static const double SAFE = 0.9, ALPHA_INC = 0.2, ALPHA_DEC = 0.25, MIN_SCALE = 0.2, MAX_SCALE = 10;
+
+/* OptRodas34::Rodas34Solve (OptRodas34.C:291-882), constants OptRodas34.H:105-149 */
+static double rodas34_attempt(cellctx* c, double dx, double invdx, double* y0, double* yTemp)
+{
+    const orc_mech* m = c->m; ws_t* w = c->w; const int n = m->n;
+    double *k1 = w->vec[0], *k2 = w->vec[1], *k3 = w->vec[2], *k4 = w->vec[3], *k5 = w->vec[4];
+    double *dy = w->vec[5], *err = w->vec[6], *dydx = w->vec[7], *dfdx = w->vec[8];
+    const double c2 = 0.386, c3 = 0.21, c4 = 0.63;
+    const double d1 = 0.25, d2 = -0.1043, d3 = 0.1035, d4 = -0.3620000000000023e-01;
+    const double a21 = 0.1544e1, a31 = 0.9466785280815826, a32 = 0.2557011698983284;
+    const double a41 = 0.3314825187068521e1, a42 = 0.2896124015972201e1, a43 = 0.9986419139977817;
+    const double a51 = 0.1221224509226641e1, a52 = 0.6019134481288629e1, a53 = 0.1253708332932087e2, a54 = -0.6878860361058950;
+    const double c21 = -0.56688e1, c31 = -0.2430093356833875e1, c32 = -0.2063599157091915;
+    const double c41 = -0.1073529058151375, c42 = -0.9594562251023355e1, c43 = -0.2047028614809616e2;
+    const double c51 = 0.7496443313967647e1, c52 = -0.1024680431464352e2, c53 = -0.3399990352819905e2, c54 = 0.1170890893206160e2;
+    const double c61 = 0.8083246795921522e1, c62 = -0.7981132988064893e1, c63 = -0.3152159432874371e2, c64 = 0.1631930543123136e2, c65 = -0.6058818238834054e1;
+    const double invgamma = 1.0 / 0.25;
+    (void)c2; (void)c3; (void)c4;
+    double* a = w->a;
+    jacobian(m, w, c->o, c->p, y0, dfdx, a);
+    for (int i = 0; i < n * n; i++) a[i] = -a[i];
+    for (int i = 0; i < n; i++) a[i * n + i] += 1.0 * invdx * invgamma;
+    lu_decompose(a, n, w->piv, w->invD);
+    w->cnt[ORC_LU]++;
+    const double dxd1 = dx * d1 + 1;
+    for (int i = 0; i < n; i++) k1[i] = dxd1 * dfdx[i];
+    lu_solve(a, n, w->piv, w->invD, k1);
+    for (int i = 0; i < n; i++) yTemp[i] = fma(a21, k1[i], y0[i]);
+    derivatives(m, w, c->p, yTemp, dydx, 1);
+    {
+        const double dxd2 = dx * d2, e1 = c21 * invdx;
+        for (int i = 0; i < n; i++) k2[i] = fma(e1, k1[i], fma(dxd2, dfdx[i], dydx[i]));
+    }
+    lu_solve(a, n, w->piv, w->invD, k2);
+    for (int i = 0; i < n; i++) yTemp[i] = fma(a32, k2[i], fma(a31, k1[i], y0[i]));
+    derivatives(m, w, c->p, yTemp, dydx, 1);
+    {
+        const double dxd3 = dx * d3, e1 = c31 * invdx, e2 = c32 * invdx;
+        for (int i = 0; i < n; i++) k3[i] = fma(e2, k2[i], fma(e1, k1[i], fma(dxd3, dfdx[i], dydx[i])));
+    }
+    lu_solve(a, n, w->piv, w->invD, k3);
+    for (int i = 0; i < n; i++) yTemp[i] = fma(a43, k3[i], fma(a42, k2[i], fma(a41, k1[i], y0[i])));
+    derivatives(m, w, c->p, yTemp, dydx, 1);
+    {
+        const double dxd4 = dx * d4, e1 = c41 * invdx, e2 = c42 * invdx, e3 = c43 * invdx;
+        for (int i = 0; i < n; i++)
+            k4[i] = fma(e3, k3[i], fma(e2, k2[i], fma(e1, k1[i], fma(dxd4, dfdx[i], dydx[i]))));
+    }
+    lu_solve(a, n, w->piv, w->invD, k4);
+    for (int i = 0; i < n; i++) {
+        dy[i] = fma(a54, k4[i], fma(a53, k3[i], fma(a52, k2[i], a51 * k1[i])));
+        yTemp[i] = y0[i] + dy[i];
+    }
+    derivatives(m, w, c->p, yTemp, dydx, 1);
+    {
+        const double e1 = c51 * invdx, e2 = c52 * invdx, e3 = c53 * invdx, e4 = c54 * invdx;
+        for (int i = 0; i < n; i++)
+            k5[i] = fma(e4, k4[i], fma(e3, k3[i], fma(e2, k2[i], fma(e1, k1[i], dydx[i]))));
+    }
+    lu_solve(a, n, w->piv, w->invD, k5);
+    for (int i = 0; i < n; i++) { dy[i] += k5[i]; yTemp[i] = y0[i] + dy[i]; }
+    derivatives(m, w, c->p, yTemp, dydx, 2);
+    {
+        const double e1 = c61 * invdx, e2 = c62 * invdx, e3 = c63 * invdx, e4 = c64 * invdx, e5 = c65 * invdx;
+        for (int i = 0; i < n; i++)
+            err[i] = fma(e5, k5[i], fma(e4, k4[i], fma(e3, k3[i], fma(e2, k2[i], fma(e1, k1[i], dydx[i])))));
+    }
+    lu_solve(a, n, w->piv, w->invD, err);
+    w->cnt[ORC_SOLVES] += 6;
+    double maxErr = 0;
+    for (int i = 0; i < n; i++) {
+        yTemp[i] = y0[i] + dy[i] + err[i];
+        const double tol = c->o->abs_tol + c->o->rel_tol * fmax(fabs(y0[i]), fabs(yTemp[i]));
+        const double e = fabs(err[i]) / tol;
+        maxErr = maxErr > e ? maxErr : e;
+    }
+    return maxErr;
+}
+
+/* OptRosenbrock34::Rosenbrock34Solve (OptRosenbrock34.C:281-678), .H:127-158 */
+static double ros34_attempt(cellctx* c, double dx, double invdx, double* y0, double* yTemp)
+{
+    const orc_mech* m = c->m; ws_t* w = c->w; const int n = m->n;
+    double *k1 = w->vec[0], *k2 = w->vec[1], *k3 = w->vec[2], *k4 = w->vec[3];
+    double *err = w->vec[6], *dydx = w->vec[7], *dfdx = w->vec[8];
+    const double a21 = 2, a31 = 48.0 / 25.0, a32 = 6.0 / 25.0;
+    const double c21 = -8, c31 = 372.0 / 25.0, c32 = 12.0 / 5.0;
+    const double c41 = -112.0 / 125.0, c42 = -54.0 / 125.0, c43 = -2.0 / 5.0;
+    const double b1 = 19.0 / 9.0, b2 = 1.0 / 2.0, b3 = 25.0 / 108.0, b4 = 125.0 / 108.0;
+    const double e1 = 34.0 / 108.0, e2 = 7.0 / 36.0, e4 = 125.0 / 108.0;
+    const double d1 = 1.0 / 2.0, d2 = -3.0 / 2.0, d3 = 605.0 / 250.0, d4 = 29.0 / 250.0;
+    const double invgamma = 1.0 / (1.0 / 2.0);
+    double* a = w->a;
+    jacobian(m, w, c->o, c->p, y0, dfdx, a);
+    for (int i = 0; i < n * n; i++) a[i] = -a[i];
+    for (int i = 0; i < n; i++) a[i * n + i] += invdx * invgamma;
+    lu_decompose(a, n, w->piv, w->invD);
+    w->cnt[ORC_LU]++;
+    const double dxd1 = dx * d1 + 1;
+    for (int i = 0; i < n; i++) k1[i] = dxd1 * dfdx[i];
+    lu_solve(a, n, w->piv, w->invD, k1);
+    for (int i = 0; i < n; i++) yTemp[i] = fma(a21, k1[i], y0[i]);
+    derivatives(m, w, c->p, yTemp, dydx, 1);
+    {
+        const double dxd2 = dx * d2, f1 = c21 * invdx;
+        for (int i = 0; i < n; i++) k2[i] = fma(f1, k1[i], fma(dxd2, dfdx[i], dydx[i]));
+    }
+    lu_solve(a, n, w->piv, w->invD, k2);
+    for (int i = 0; i < n; i++) yTemp[i] = fma(a32, k2[i], fma(a31, k1[i], y0[i]));
+    derivatives(m, w, c->p, yTemp, dydx, 1);
+    {
+        const double dxd3 = dx * d3, f1 = c31 * invdx, f2 = c32 * invdx;
+        for (int i = 0; i < n; i++) k3[i] = fma(f2, k2[i], fma(f1, k1[i], fma(dxd3, dfdx[i], dydx[i])));
+    }
+    lu_solve(a, n, w->piv, w->invD, k3);
+    {
+        const double dxd4 = dx * d4, f1 = c41 * invdx, f2 = c42 * invdx, f3 = c43 * invdx;
+        for (int i = 0; i < n; i++)
+            k4[i] = fma(f3, k3[i], fma(f2, k2[i], fma(f1, k1[i], fma(dxd4, dfdx[i], dydx[i]))));
+    }
+    lu_solve(a, n, w->piv, w->invD, k4);
+    w->cnt[ORC_SOLVES] += 4;
+    double maxErr = 0;
+    for (int i = 0; i < n; i++) {
+        yTemp[i] = fma(b4, k4[i], fma(b3, k3[i], fma(b2, k2[i], fma(b1, k1[i], y0[i]))));
+        err[i] = fma(e4, k4[i], fma(e2, k2[i], e1 * k1[i]));
+        const double tol = c->o->abs_tol + c->o->rel_tol * fmax(fabs(y0[i]), fabs(yTemp[i]));
+        const double e = fabs(err[i]) / tol;
+        maxErr = maxErr > e ? maxErr : e;
+    }
+    return maxErr;
+}
+
+/* ODESolve + adaptiveSolve (OptRodas34.C:123-289, OptRosenbrock34.C:127-279) */
+static int rosenbrock_integrate(cellctx* c, double xEnd, double* dxTryIO, double* y0)
+{
+    const double ratio = pow(MAX_SCALE / SAFE, -1.0 / ALPHA_INC);
+    const double safeMaxScale = SAFE * MAX_SCALE;
+    ws_t* w = c->w;
+    double* yTemp = w->vec[9];
+    const int n = c->m->n;
+    double dxTry = *dxTryIO;
+    int last = 0;
+    double x = 0;
+    for (int nStep = 0; nStep < c->o->max_steps; nStep++) {
+        const double dxTry0 = dxTry;
+        if ((x + dxTry - xEnd) * (x + dxTry - 0.0) > 0) { last = 1; dxTry = xEnd - x; }
+        double dx = dxTry, invdx = 1.0 / dx;
+        double Err = c->o->solver == FCS_SOLVER_RODAS34 ? rodas34_attempt(c, dx, invdx, y0, yTemp)
+                                                        : ros34_attempt(c, dx, invdx, y0, yTemp);
+        w->cnt[ORC_ATTEMPTS]++;
+        int rejects = 0;
+        while (Err > 1) {
+            if (++rejects > 100000) return FCS_CELL_DT_UNDERFLOW;
+            const double scale = fmax(SAFE * pow(Err, -ALPHA_DEC), MIN_SCALE);
+            dx *= scale;
+            invdx = 1.0 / dx;
+            Err = c->o->solver == FCS_SOLVER_RODAS34 ? rodas34_attempt(c, dx, invdx, y0, yTemp)
+                                                     : ros34_attempt(c, dx, invdx, y0, yTemp);
+            w->cnt[ORC_ATTEMPTS]++;
+        }
+        if (!(Err == Err)) return FCS_CELL_NONFINITE;
+        w->cnt[ORC_ACCEPTED]++;
+        x += dx;
+        for (int i = 0; i < n; i++) y0[i] = yTemp[i];
+        dxTry = (Err > ratio) ? fmin(fmax(SAFE * pow(Err, -ALPHA_INC), MIN_SCALE), MAX_SCALE) * dx
+                              : safeMaxScale * dx;
+        if ((x - xEnd) * (xEnd - 0.0) >= 0) {
+            if (nStep > 0 && last) dxTry = dxTry0;
+            *dxTryIO = dxTry;
+            return FCS_CELL_OK;
+        }
+    }
+    return FCS_CELL_MAX_STEPS;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Seulex: OptSeulex.C:34-94 (setup), 171-260, 262-560, 562-709, 711-734     */
+
+#define KMAXX 12
+#define IMAXX (KMAXX + 1)
+
+typedef struct {
+    double jacRedo, theta, logTol;
+    int kTarg;
+    int nSeq[IMAXX];
+    double cpu[IMAXX], coeff[IMAXX][IMAXX];
+    double dxOpt[IMAXX], temp[IMAXX];
+} seulex_t;
+
+static void seulex_init(seulex_t* s, const orc_options* o)
+{
+    s->jacRedo = fmin(1e-4, o->rel_tol);
+    s->theta = 2 * s->jacRedo;
+    const double cpuFunc = 1, cpuJac = 5, cpuLU = 1, cpuSolve = 1;
+    s->nSeq[0] = 2; s->nSeq[1] = 3;
+    for (int i = 2; i < IMAXX; i++) s->nSeq[i] = 2 * s->nSeq[i - 2];
+    s->cpu[0] = cpuJac + cpuLU + s->nSeq[0] * (cpuFunc + cpuSolve);
+    for (int k = 0; k < KMAXX; k++)
+        s->cpu[k + 1] = s->cpu[k] + (s->nSeq[k + 1] - 1) * (cpuFunc + cpuSolve) + cpuLU;
+    for (int k = 0; k < IMAXX; k++)
+        for (int l = 0; l < k; l++) {
+            const double r = (double)s->nSeq[k] / s->nSeq[l];
+            s->coeff[k][l] = 1 / (r - 1);
+        }
+    s->logTol = -log10(o->rel_tol + o->abs_tol) * 0.6 + 0.5;
+}
+
+static int seul(cellctx* c, seulex_t* s, double x0, double* y0, double dxTot, int k,
+                double* ySeq, double* scale)
+{
+    const orc_mech* m = c->m; ws_t* w = c->w; const int n = m->n;
+    double *yTemp = w->vec[10], *dy = w->vec[11], *dydx = w->vec[12];
+    const int nSteps = s->nSeq[k];
+    const double dx = dxTot / nSteps;
+    (void)dx;
+    const double invdx = nSteps / dxTot;
+    double* a = w->a;
+    const double* Jy = w->Jy;
+    for (int i = 0; i < n * n; i++) a[i] = -Jy[i];
+    for (int i = 0; i < n; i++) a[i * n + i] += invdx;
+    lu_decompose(a, n, w->piv, w->invD);
+    w->cnt[ORC_LU]++;
+    (void)x0;
+    derivatives(m, w, c->p, y0, dy, 1);
+    lu_solve(a, n, w->piv, w->invD, dy);
+    w->cnt[ORC_SOLVES]++;
+    for (int i = 0; i < n; i++) yTemp[i] = y0[i];
+    for (int nn = 1; nn < nSteps; nn++) {
+        for (int i = 0; i < n; i++) yTemp[i] += dy[i];
+        if (nn == 1 && k <= 1) {
+            double dy1 = 0;
+            for (int i = 0; i < n; i++) { const double q = dy[i] / scale[i]; dy1 += q * q; }
+            dy1 = sqrt(dy1);
+            derivatives(m, w, c->p, yTemp, dydx, 1);
+            for (int i = 0; i < n; i++) dy[i] = dydx[i] - dy[i] * invdx;
+            lu_solve(a, n, w->piv, w->invD, dy);
+            w->cnt[ORC_SOLVES]++;
+            double dy2 = 0.0;
+            for (int i = 0; i < n; i++) {
+                if (fabs(dy[i]) > sqrt(VGREAT)) { dy2 = VGREAT; break; }
+                const double q = dy[i] / scale[i];
+                dy2 += q * q;
+            }
+            dy2 = sqrt(dy2);
+            s->theta = dy2 / fmax(1.0, dy1 + SMALL);
+            if (s->theta > 1.0) return 0;
+        }
+        derivatives(m, w, c->p, yTemp, dy, 1);
+        lu_solve(a, n, w->piv, w->invD, dy);
+        w->cnt[ORC_SOLVES]++;
+    }
+    for (int i = 0; i < n; i++) ySeq[i] = yTemp[i] + dy[i];
+    return 1;
+}
+
+static void extrapolate(seulex_t* s, int k, double* table, int n, double* y)
+{
+    for (int j = k - 1; j > 0; j--)
+        for (int i = 0; i < n; i++)
+            table[(j - 1) * n + i] = table[j * n + i] + s->coeff[k][j] * (table[j * n + i] - table[(j - 1) * n + i]);
+    for (int i = 0; i < n; i++) y[i] = table[i] + s->coeff[k][0] * (table[i] - y[i]);
+}
+
+typedef struct { double dxTry, dxDid; int first, last, reject, prevReject; } sstep_t;
+
+static void seulex_step(cellctx* c, seulex_t* s, double* x, sstep_t* st, double* y)
+{
+    const orc_mech* m = c->m; ws_t* w = c->w; const int n = m->n;
+    double *y0_ = w->vec[0], *ySeq = w->vec[1], *scale = w->vec[2], *k9 = w->vec[3];
+    double* table = w->table;
+    s->temp[0] = 1e15; /* great */
+    double dx = st->dxTry;
+    for (int i = 0; i < n; i++) y0_[i] = y[i];
+    s->dxOpt[0] = fabs(0.1 * dx);
+    if (st->first || st->prevReject) s->theta = 2 * s->jacRedo;
+    if (st->first) {
+        int kt = (int)s->logTol;
+        kt = kt < KMAXX - 1 ? kt : KMAXX - 1;
+        s->kTarg = kt > 1 ? kt : 1;
+    }
+    for (int i = 0; i < n; i++) scale[i] = c->o->abs_tol + c->o->rel_tol * fabs(y[i]);
+    int jacUpdated = 0;
+    if (s->theta > s->jacRedo) {
+        jacobian(m, w, c->o, c->p, y, k9, w->Jy);
+        jacUpdated = 1;
+    }
+    int k = 0;
+    double dxNew = fabs(dx);
+    int firstk = 1;
+    while (firstk || st->reject) {
+        dx = dxNew;
+        firstk = 0;
+        st->reject = 0;
+        double errOld = 0;
+        for (k = 0; k <= s->kTarg + 1; k++) {
+            w->cnt[ORC_ATTEMPTS] += (k == 0);
+            int ok = seul(c, s, *x, y0_, dx, k, ySeq, scale);
+            if (!ok) { st->reject = 1; dxNew = fabs(dx) * 0.5; break; }
+            if (k == 0) for (int i = 0; i < n; i++) y[i] = ySeq[i];
+            else for (int i = 0; i < n; i++) table[(k - 1) * n + i] = ySeq[i];
+            if (k != 0) {
+                extrapolate(s, k, table, n, y);
+                double err = 0;
+                for (int i = 0; i < n; i++) {
+                    scale[i] = c->o->abs_tol + c->o->rel_tol * fabs(y0_[i]);
+                    const double q = (y[i] - table[i]) / scale[i];
+                    err += q * q;
+                }
+                err = sqrt(err / n);
+                if (err > 1 / SMALL || (k > 1 && err >= errOld)) { st->reject = 1; dxNew = fabs(dx) * 0.5; break; }
+                errOld = fmin(4 * err, 1);
+                const double expo = 1.0 / (k + 1);
+                const double facmin = pow(0.1, expo);
+                double fac;
+                if (err == 0) fac = 1.0 / facmin;
+                else {
+                    fac = 0.93 / pow(err / 0.8, expo);
+                    fac = fmax(facmin / 4, fmin(1 / facmin, fac));
+                }
+                s->dxOpt[k] = fabs(dx * fac);
+                s->temp[k] = s->cpu[k] / s->dxOpt[k];
+                if ((st->first || st->last) && err <= 1.0) break;
+                if (k == s->kTarg - 1 && !st->prevReject && !st->first && !st->last) {
+                    if (err <= 1.0) break;
+                    else if (err > s->nSeq[s->kTarg] * s->nSeq[s->kTarg + 1] * 4.0) {
+                        st->reject = 1;
+                        s->kTarg = k;
+                        if (s->kTarg > 1 && s->temp[k - 1] < 0.7 * s->temp[k]) s->kTarg--;
+                        dxNew = s->dxOpt[s->kTarg];
+                        break;
+                    }
+                }
+                if (k == s->kTarg) {
+                    if (err <= 1.0) break;
+                    else if (err > s->nSeq[k + 1] * 2.0) {
+                        st->reject = 1;
+                        if (s->kTarg > 1 && s->temp[k - 1] < 0.7 * s->temp[k]) s->kTarg--;
+                        dxNew = s->dxOpt[s->kTarg];
+                        break;
+                    }
+                }
+                if (k == s->kTarg + 1) {
+                    if (err > 1.0) {
+                        st->reject = 1;
+                        if (s->kTarg > 1 && s->temp[s->kTarg - 1] < 0.7 * s->temp[s->kTarg]) s->kTarg--;
+                        dxNew = s->dxOpt[s->kTarg];
+                    }
+                    break;
+                }
+            }
+        }
+        if (st->reject) {
+            st->prevReject = 1;
+            if (!jacUpdated) {
+                s->theta = 2.0 * s->jacRedo;
+                if (s->theta > s->jacRedo && !jacUpdated) {
+                    jacobian(m, w, c->o, c->p, y, k9, w->Jy);
+                    jacUpdated = 1;
+                }
+            }
+        }
+    }
+    st->dxDid = dx;
+    *x += dx;
+    int kopt;
+    if (k == 1) kopt = 2;
+    else if (k <= s->kTarg) {
+        kopt = k;
+        if (s->temp[k - 1] < 0.7 * s->temp[k]) kopt = k - 1;
+        else if (s->temp[k] < 0.9 * s->temp[k - 1]) kopt = (k + 1 < KMAXX - 1) ? k + 1 : KMAXX - 1;
+    } else {
+        kopt = k - 1;
+        if (k > 2 && s->temp[k - 2] < 0.7 * s->temp[k - 1]) kopt = k - 2;
+        if (s->temp[k] < 0.9 * s->temp[kopt]) kopt = (k < KMAXX - 1) ? k : KMAXX - 1;
+    }
+    if (st->prevReject) {
+        s->kTarg = kopt < k ? kopt : k;
+        dxNew = fmin(fabs(dx), s->dxOpt[s->kTarg]);
+        st->prevReject = 0;
+    } else {
+        if (kopt <= k) dxNew = s->dxOpt[kopt];
+        else {
+            if (k < s->kTarg && s->temp[k] < 0.9 * s->temp[k - 1]) dxNew = s->dxOpt[k] * s->cpu[kopt + 1] / s->cpu[k];
+            else dxNew = s->dxOpt[k] * s->cpu[kopt] / s->cpu[k];
+        }
+        s->kTarg = kopt;
+    }
+    st->dxTry = dxNew;
+}
+
+static int seulex_integrate(cellctx* c, seulex_t* s, double xEnd, double* dxTryIO, double* y0)
+{
+    ws_t* w = c->w;
+    sstep_t st = {*dxTryIO, 0, 1, 0, 0, 0};
+    double x = 0;
+    for (int nStep = 0; nStep < c->o->max_steps; nStep++) {
+        const double dxTry0 = st.dxTry;
+        st.reject = 0;
+        if ((x + st.dxTry - xEnd) * (x + st.dxTry - 0.0) > 0) { st.last = 1; st.dxTry = xEnd - x; }
+        seulex_step(c, s, &x, &st, y0);
+        w->cnt[ORC_ACCEPTED]++;
+        for (int i = 0; i < c->m->n; i++) if (!(y0[i] == y0[i])) return FCS_CELL_NONFINITE;
+        if ((x - xEnd) * (xEnd - 0.0) >= 0) {
+            if (nStep > 0 && st.last) st.dxTry = dxTry0;
+            *dxTryIO = st.dxTry;
+            return FCS_CELL_OK;
+        }
+        st.first = 0;
+        if (st.reject) st.prevReject = 1;
+    }
+    return FCS_CELL_MAX_STEPS;
+}
+
+/* ------------------------------------------------------------------------ */
+/* cell loop: FastChemistryModel_transientSolve.H:30-104                     */
+
+typedef struct {
+    const orc_mech* m; const orc_options* o;
+    int64_t n; double dt; const double* dtc;
+    const double *p, *rho0; double *T, *Y, *subDt, *RR; int32_t* status;
+    double* dtMinCell;
+    volatile int64_t next;
+    pthread_mutex_t lock;
+    int64_t counters[ORC_NCOUNTERS];
+} job_t;
+
+static void* worker(void* arg)
+{
+    job_t* j = (job_t*)arg;
+    const orc_mech* m = j->m;
+    const int ns = m->ns, n = m->n;
+    ws_t* w = ws_create(m);
+    double* y = (double*)malloc(sizeof(double) * n);
+    double* Y0 = (double*)malloc(sizeof(double) * ns);
+    seulex_t sx;
+    seulex_init(&sx, j->o);
+    for (;;) {
+        int64_t c0 = __atomic_fetch_add((int64_t*)&j->next, 16, __ATOMIC_RELAXED);
+        if (c0 >= j->n) break;
+        int64_t c1 = c0 + 16 < j->n ? c0 + 16 : j->n;
+        for (int64_t c = c0; c < c1; c++) {
+            const double deltaT = j->dtc ? j->dtc[c] : j->dt;
+            double T = j->T[c];
+            j->dtMinCell[c] = 1e300;
+            if (!(T > j->o->T_react)) {
+                if (j->RR) for (int i = 0; i < ns; i++) j->RR[(size_t)i * j->n + c] = 0;
+                if (j->status) j->status[c] = FCS_CELL_SKIPPED;
+                continue;
+            }
+            for (int i = 0; i < ns; i++) Y0[i] = j->Y[(size_t)i * j->n + c];
+            double subDt = j->subDt[c];
+            cellctx cc = {m, w, j->o, j->p[c]};
+            int st = FCS_CELL_OK;
+            double timeLeft = deltaT;
+            /* Y_ = Y0; solve(p, T, Y_, li, dt, subDt) */
+            for (int i = 0; i < ns; i++) y[i] = Y0[i] > 0 ? Y0[i] : 0;
+            y[ns] = T;
+            while (timeLeft > SMALL) {
+                double dtc = timeLeft;
+                if (j->o->solver == FCS_SOLVER_SEULEX) st = seulex_integrate(&cc, &sx, dtc, &subDt, y);
+                else st = rosenbrock_integrate(&cc, dtc, &subDt, y);
+                timeLeft -= dtc;
+                if (st != FCS_CELL_OK) break;
+            }
+            w->cnt[ORC_CELLS]++;
+            if (st != FCS_CELL_OK) w->cnt[ORC_FAILED]++;
+            for (int i = 0; i < ns; i++) {
+                const double Yn = y[i] > 0 ? y[i] : 0.0;
+                j->Y[(size_t)i * j->n + c] = Yn;
+                if (j->RR) j->RR[(size_t)i * j->n + c] = (Yn * j->rho0[c] - Y0[i] * j->rho0[c]) / deltaT;
+            }
+            j->T[c] = y[ns];
+            j->dtMinCell[c] = subDt;
+            j->subDt[c] = subDt < j->o->delta_t_chem_max ? subDt : j->o->delta_t_chem_max;
+            if (j->status) j->status[c] = st;
+        }
+    }
+    pthread_mutex_lock(&j->lock);
+    for (int i = 0; i < ORC_NCOUNTERS; i++) j->counters[i] += w->cnt[i];
+    pthread_mutex_unlock(&j->lock);
+    free(y); free(Y0);
+    ws_destroy(w);
+    return NULL;
+}
+
+void orc_default_options(orc_options* o)
+{
+    o->solver = FCS_SOLVER_RODAS34;
+    o->jacobian = FCS_JACOBIAN_EXACT;
+    o->conversion_as_written = 0;
+    o->max_steps = 10000;
+    o->abs_tol = 1e-8;
+    o->rel_tol = 1e-4;
+    o->T_react = 0.0;
+    o->delta_t_chem_max = 1e300;
+    o->n_threads = 1;
+}
+
+int32_t orc_integrate(const orc_mech* m, const orc_options* o, int64_t n_cells,
+                      double delta_t, const double* dtc, const double* p, const double* rho0,
+                      double* T, double* Y, double* sub_dt, double* RR, int32_t* cell_status,
+                      double* delta_t_min, int64_t* counters)
+{
+    job_t j;
+    memset(&j, 0, sizeof(j));
+    j.m = m; j.o = o; j.n = n_cells; j.dt = delta_t; j.dtc = dtc;
+    j.p = p; j.rho0 = rho0; j.T = T; j.Y = Y; j.subDt = sub_dt; j.RR = RR; j.status = cell_status;
+    j.dtMinCell = (double*)malloc(sizeof(double) * (n_cells > 0 ? n_cells : 1));
+    pthread_mutex_init(&j.lock, NULL);
+    int nt = o->n_threads > 0 ? o->n_threads : 1;
+    if (nt == 1) worker(&j);
+    else {
+        pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nt);
+        for (int t = 0; t < nt; t++) pthread_create(&th[t], NULL, worker, &j);
+        for (int t = 0; t < nt; t++) pthread_join(th[t], NULL);
+        free(th);
+    }
+    pthread_mutex_destroy(&j.lock);
+    double dmin = 1e15; /* great */
+    for (int64_t c = 0; c < n_cells; c++) if (j.dtMinCell[c] < dmin) dmin = j.dtMinCell[c];
+    free(j.dtMinCell);
+    const double dtref = dtc ? dtc[0] : delta_t;
+    if (delta_t_min) *delta_t_min = dmin < 2 * dtref ? dmin : 2 * dtref;
+    if (counters) for (int i = 0; i < ORC_NCOUNTERS; i++) counters[i] = j.counters[i];
+    return j.counters[ORC_FAILED] ? FCS_ERR_CELLS : FCS_OK;
+}
+
+int32_t orc_rhs(const orc_mech* m, int64_t n_cells, const double* p, const double* T,
+                const double* Y, double* dydt)
+{
+    ws_t* w = ws_create(m);
+    const int ns = m->ns, n = m->n;
+    double* y = (double*)malloc(sizeof(double) * n);
+    double* f = (double*)malloc(sizeof(double) * n);
+    for (int64_t c = 0; c < n_cells; c++) {
+        for (int i = 0; i < ns; i++) y[i] = Y[(size_t)i * n_cells + c];
+        y[ns] = T[c];
+        derivatives(m, w, p[c], y, f, 1);
+        for (int i = 0; i < n; i++) dydt[(size_t)i * n_cells + c] = f[i];
+    }
+    free(y); free(f);
+    ws_destroy(w);
+    return FCS_OK;
+}
+
+int32_t orc_jacobian(const orc_mech* m, const orc_options* o, int64_t n_cells,
+                     const double* p, const double* T, const double* Y, double* J, double* dydt)
+{
+    ws_t* w = ws_create(m);
+    const int ns = m->ns, n = m->n;
+    double* y = (double*)malloc(sizeof(double) * n);
+    double* f = (double*)malloc(sizeof(double) * n);
+    for (int64_t c = 0; c < n_cells; c++) {
+        for (int i = 0; i < ns; i++) y[i] = Y[(size_t)i * n_cells + c];
+        y[ns] = T[c];
+        jacobian(m, w, o, p[c], y, f, &J[(size_t)c * n * n]);
+        for (int i = 0; i < n; i++) dydt[(size_t)i * n_cells + c] = f[i];
+    }
+    free(y); free(f);
+    ws_destroy(w);
+    return FCS_OK;
+}
