@@ -56,14 +56,14 @@ struct fcs_ctx {
     int numSMs = 0;
     size_t maxSmemPerBlock = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evc0 = nullptr, evc1 = nullptr;
     std::string err;
     // mechanism
     bool loaded = false;
     DevMech M{};
     DBuf<double> dW, dInvW, dTc, dCoef, dEff, dPlogRow, dPlogTa, dHf;
     DBuf<RxnInfo> dRx;
-    DBuf<int> dPlogOff, dIncOff, dInc;
+    DBuf<int> dPlogOff, dIncOff, dInc, dTbInc;
     // options
     fcs_options opt{};
     // per-call buffers
@@ -120,7 +120,8 @@ extern "C" fcs_status fcs_create(fcs_ctx** out, int device) {
     cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     ctx->maxSmemPerBlock = (size_t)v;
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
+        cudaEventCreate(&ctx->evc0) != cudaSuccess || cudaEventCreate(&ctx->evc1) != cudaSuccess) {
         delete ctx;
         return FCS_ERR_CUDA;
     }
@@ -138,11 +139,13 @@ extern "C" fcs_status fcs_destroy(fcs_ctx* ctx) {
                             &ctx->bSub, &ctx->bRR, &ctx->bDt, &ctx->bOut, &ctx->bJ, &ctx->bQ})
         b->release();
     ctx->dRx.release();
-    ctx->dPlogOff.release(); ctx->dIncOff.release(); ctx->dInc.release();
+    ctx->dPlogOff.release(); ctx->dIncOff.release(); ctx->dInc.release(); ctx->dTbInc.release();
     ctx->bStatus.release(); ctx->bOrder.release(); ctx->bHead.release();
     ctx->bStats.release(); ctx->bMin.release(); ctx->gws.release();
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->evc0) cudaEventDestroy(ctx->evc0);
+    if (ctx->evc1) cudaEventDestroy(ctx->evc1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return FCS_OK;
@@ -180,7 +183,8 @@ extern "C" fcs_status fcs_mechanism_size(const fcs_ctx* ctx, int32_t* ns, int32_
 extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc* d) {
     if (!ctx || !d) return FCS_ERR_INVALID;
     const int ns = d->n_species, nr = d->n_reactions;
-    if (ns < 1 || nr < 0 || ns > 32000) return set_err(ctx, FCS_ERR_INVALID, "bad species/reaction count");
+    if (ns < 1 || nr < 0) return set_err(ctx, FCS_ERR_INVALID, "bad species/reaction count");
+    if (ns > 255) return set_err(ctx, FCS_ERR_UNSUPPORTED, "the GPU path handles up to 255 species");
     if (!d->W || !d->T_low || !d->T_high || !d->T_common || !d->high_coeffs || !d->low_coeffs)
         return set_err(ctx, FCS_ERR_INVALID, "missing species arrays");
     if (nr > 0 && (!d->type || !d->reversible || !d->lhs_offset || !d->lhs_species || !d->rhs_offset ||
@@ -226,6 +230,7 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
     std::vector<int> plogOff{0};
     std::vector<double> plogRow, plogTa;
     std::vector<std::vector<int>> inc(ns);
+    std::vector<int> tbInc;
     int nTB = 0, nPlog = 0;
     for (int k = 0; k < nr; k++) {
         const int r = order[k];
@@ -265,6 +270,8 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
             if (!d->efficiencies) return set_err(ctx, FCS_ERR_INVALID, "third-body reaction without efficiencies");
             for (int s = 0; s < ns; s++) eff.push_back(d->efficiencies[(size_t)r * ns + s]);
             x.tb = nTB++;
+            for (int q = 0; q < x.nl; q++) tbInc.push_back((int(x.sl[q]) << 16) | (x.tb << 1));
+            for (int q = 0; q < x.nr; q++) tbInc.push_back((int(x.sr[q]) << 16) | (x.tb << 1) | 1);
         }
         if (d->type[r] == FCS_RXN_PLOG) {
             if (!d->plog_offset || !d->plog_table) return set_err(ctx, FCS_ERR_INVALID, "PLOG reaction without table");
@@ -289,6 +296,9 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
         incv.insert(incv.end(), inc[i].begin(), inc[i].end());
     }
     if (incv.empty()) incv.push_back(0);
+    const int nTbInc = (int)tbInc.size();
+    if (tbInc.empty()) tbInc.push_back(0);
+    if (nTB >= 32768) return set_err(ctx, FCS_ERR_UNSUPPORTED, "too many third-body reactions");
     if (eff.empty()) eff.push_back(0);
     if (plogRow.empty()) { plogRow.assign(4, 0); plogTa.assign(1, 0); }
     cudaSetDevice(ctx->device);
@@ -300,13 +310,14 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
     CK(up(ctx->dW, W)); CK(up(ctx->dInvW, invW)); CK(up(ctx->dTc, Tc)); CK(up(ctx->dCoef, coef));
     CK(up(ctx->dRx, rx)); CK(up(ctx->dEff, eff)); CK(up(ctx->dPlogOff, plogOff));
     CK(up(ctx->dPlogRow, plogRow)); CK(up(ctx->dPlogTa, plogTa)); CK(up(ctx->dIncOff, incOff));
-    CK(up(ctx->dInc, incv)); CK(up(ctx->dHf, hf));
+    CK(up(ctx->dInc, incv)); CK(up(ctx->dHf, hf)); CK(up(ctx->dTbInc, tbInc));
     DevMech& M = ctx->M;
     M.ns = ns; M.n = ns + 1; M.nr = nr; M.nTB = nTB; M.nPlog = nPlog;
     M.TlowMin = TlowMin; M.ThighMax = ThighMax; M.TcommonMin = TcMin; M.TcommonMax = TcMax;
     M.W = ctx->dW.p; M.invW = ctx->dInvW.p; M.Tcommon = ctx->dTc.p; M.coef = ctx->dCoef.p;
     M.rx = ctx->dRx.p; M.eff = ctx->dEff.p; M.plogOff = ctx->dPlogOff.p; M.plogRow = ctx->dPlogRow.p;
     M.plogTa = ctx->dPlogTa.p; M.incOff = ctx->dIncOff.p; M.inc = ctx->dInc.p; M.hf = ctx->dHf.p;
+    M.nTbInc = nTbInc; M.tbInc = ctx->dTbInc.p;
     ctx->loaded = true;
     ctx->tuned.clear();
     return FCS_OK;
@@ -333,11 +344,10 @@ static bool make_shape(fcs_ctx* ctx, int group, bool integrate, Shape& sh) {
     const fcs_options& o = ctx->opt;
     const bool mixed = o.precision == FCS_PRECISION_MIXED;
     const bool seulex = integrate && o.solver == FCS_SOLVER_SEULEX;
-    const bool two = mixed || seulex;
     sh.mixed = mixed;
-    sh.L = make_layout(ctx->M.ns, ctx->M.nr, ctx->M.nTB, mixed ? 4 : 8, two, seulex);
+    sh.L = make_layout(ctx->M.ns, ctx->M.nr, ctx->M.nTB, mixed, seulex);
     sh.lc.group = group;
-    if (group == 32 && ctx->M.n > 256) return false;  // warp solves keep <= 256 unknowns in registers
+    if (ctx->M.n > 256) return false;  // the solves keep <= 256 unknowns per warp lane set
     const size_t smemCap = ctx->maxSmemPerBlock;
     int groupsPerBlock = 1;
     if (group == 32) {
@@ -397,6 +407,7 @@ static fcs_status integrate_impl(fcs_ctx* ctx, int64_t nc, double dt, const doub
     CellIO io{};
     io.nCells = nc;
     io.deltaT = dt;
+    CK(cudaEventRecord(ctx->evc0, st));
     if (dev) {
         io.p = p; io.rho0 = rho0; io.T = T; io.Y = Y; io.subDt = sub; io.RR = RR; io.status = status;
         io.dtPerCell = dtc;
@@ -451,9 +462,11 @@ static fcs_status integrate_impl(fcs_ctx* ctx, int64_t nc, double dt, const doub
         if (RR) CK(cudaMemcpyAsync(RR, io.RR, (size_t)ns * nc * 8, cudaMemcpyDeviceToHost, st));
         if (status) CK(cudaMemcpyAsync(status, io.status, nc * 4, cudaMemcpyDeviceToHost, st));
     }
+    CK(cudaEventRecord(ctx->evc1, st));
     CK(cudaStreamSynchronize(st));
-    float ms = 0;
+    float ms = 0, cms = 0;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    cudaEventElapsedTime(&cms, ctx->evc0, ctx->evc1);
     if (stats) {
         stats->cells_integrated = hs[ST_CELLS];
         stats->cells_skipped = hs[ST_SKIPPED];
@@ -464,7 +477,9 @@ static fcs_status integrate_impl(fcs_ctx* ctx, int64_t nc, double dt, const doub
         stats->lu_decompositions = hs[ST_LU];
         stats->rhs_evaluations = hs[ST_RHS];
         stats->linear_solves = hs[ST_SOLVES];
+        stats->fp64_fallbacks = hs[ST_FALLBACK];
         stats->kernel_ms = ms;
+        stats->call_ms = cms;
     }
     if (dtMin) {
         double m = 1e15;  // great
@@ -522,7 +537,7 @@ static fcs_status eval_impl(fcs_ctx* ctx, int64_t nc, const double* p, const dou
         if (J) { CK(ctx->bJ.ensure((size_t)n * n * nc)); dJ = ctx->bJ.p; }
         if (Qdot) { CK(ctx->bQ.ensure(nc)); dQ = ctx->bQ.p; }
     }
-    const int group = default_group(ctx);
+    const int group = ctx->opt.mapping ? ctx->opt.mapping : default_group(ctx);
     Shape sh;
     if (!make_shape(ctx, group, false, sh)) return set_err(ctx, FCS_ERR_UNSUPPORTED, "no launch shape");
     const int gpb = sh.lc.block / sh.lc.group;

@@ -92,11 +92,12 @@ __device__ __forceinline__ double gmax(const Grp<G>& g, double v, double* red) {
 
 struct SlotLayout {
     int ld;            // matrix leading dimension (odd: conflict-free column walks)
-    int offJ;          // Jacobian (MT)
-    int offLU;         // LU factors (MT); == offJ when factored in place
-    int offVec;        // NV vectors of n doubles
-    int offSp;         // 6 species arrays (C, B, Cp, Ha, dBdT, dCpdT) [ns]
+    int offJ64, offLU64;  // FP64 views of the Jacobian / LU factors (LU64 == J64: in place)
+    int offJ32, offLU32;  // FP32 views (mixed precision), inside the same matrix region
+    int offVec;        // kNV vectors of n doubles
+    int offSp;         // 7 species arrays (C, E, Einv, Cp, Ha, dBdT, dCpdT) [ns]
     int offInvD;       // [n] double
+    int offScale;      // row / column equilibration factors [2n] double (mixed precision)
     int offPiv;        // [n] int
     int offRx;         // Kf, Kr, q, dqdT [nr] each
     int offTb;         // M, dKfdC, dKrdC, CF, CR [nTB] each
@@ -109,26 +110,34 @@ constexpr int kNV = 16;  // stage / work vectors per slot
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 
-// mtBytes: 8 for an FP64 matrix, 4 for FP32; twoMatrices: J kept beside LU
-__host__ __device__ inline SlotLayout make_layout(int ns, int nr, int nTB, int mtBytes,
-                                                  bool twoMatrices, bool seulex) {
+// Matrix region:
+//   FP64 Rosenbrock : one FP64 matrix, factored in place
+//   FP64 Seulex     : FP64 Jacobian + FP64 LU (the Jacobian is reused across orders)
+//   mixed Rosenbrock: FP32 Jacobian + FP32 LU; the FP64 view (Jacobian assembly in
+//                     FP64, and the FP64 fallback attempt) overlays both
+//   mixed Seulex    : as FP64 Seulex, with the two FP32 matrices inside the FP64 Jacobian
+__host__ __device__ inline SlotLayout make_layout(int ns, int nr, int nTB, bool mixed, bool seulex) {
     SlotLayout L;
     const int n = ns + 1;
     L.ld = n | 1;
+    const int m64 = align16(n * L.ld * 8), m32 = align16(n * L.ld * 4);
     int o = 0;
-    L.offJ = o;
-    o = align16(o + n * L.ld * mtBytes);
-    if (twoMatrices) { L.offLU = o; o = align16(o + n * L.ld * mtBytes); }
-    else L.offLU = L.offJ;
-    L.offVec = o;  o = align16(o + kNV * n * 8);
-    L.offSp = o;   o = align16(o + 6 * ns * 8);
-    L.offInvD = o; o = align16(o + n * 8);
-    L.offPiv = o;  o = align16(o + n * 4);
-    L.offRx = o;   o = align16(o + 4 * nr * 8);
-    L.offTb = o;   o = align16(o + 5 * (nTB > 0 ? nTB : 1) * 8);
+    L.offJ64 = 0;
+    if (seulex) { L.offLU64 = m64; o = 2 * m64; }
+    else if (mixed) { L.offLU64 = 0; o = 2 * m32 > m64 ? 2 * m32 : m64; }
+    else { L.offLU64 = 0; o = m64; }
+    L.offJ32 = 0;
+    L.offLU32 = m32;
+    L.offVec = o;   o = align16(o + kNV * n * 8);
+    L.offSp = o;    o = align16(o + 7 * ns * 8);
+    L.offInvD = o;  o = align16(o + n * 8);
+    L.offScale = o; o = align16(o + 2 * n * 8);
+    L.offPiv = o;   o = align16(o + n * 4);
+    L.offRx = o;    o = align16(o + 4 * nr * 8);
+    L.offTb = o;    o = align16(o + 5 * (nTB > 0 ? nTB : 1) * 8);
     L.offTable = o;
     if (seulex) o = align16(o + 12 * n * 8);
-    L.offRed = o;  o = align16(o + 48 * 8);
+    L.offRed = o;   o = align16(o + 48 * 8);
     L.bytes = o;
     return L;
 }
@@ -139,8 +148,9 @@ struct Slot {
     MT* J;
     MT* LU;
     double* vec;      // vec + k*n is vector k
-    double *C, *B, *Cp, *Ha, *dBdT, *dCpdT;
+    double *C, *B, *Binv, *Cp, *Ha, *dBdT, *dCpdT;   // B = exp(-G/RT), Binv = 1/B
     double* invD;
+    double *dr, *dc;
     int* piv;
     double *Kf, *Kr, *q, *dqdT;
     double *Mtb, *tbF, *tbR, *tbCF, *tbCR;
@@ -153,13 +163,20 @@ template<class MT>
 __device__ __forceinline__ Slot<MT> make_slot(char* base, const SlotLayout& L, const DevMech& M) {
     Slot<MT> s;
     s.ld = L.ld; s.n = M.n; s.ns = M.ns;
-    s.J = reinterpret_cast<MT*>(base + L.offJ);
-    s.LU = reinterpret_cast<MT*>(base + L.offLU);
+    if constexpr (sizeof(MT) == 8) {
+        s.J = reinterpret_cast<MT*>(base + L.offJ64);
+        s.LU = reinterpret_cast<MT*>(base + L.offLU64);
+    } else {
+        s.J = reinterpret_cast<MT*>(base + L.offJ32);
+        s.LU = reinterpret_cast<MT*>(base + L.offLU32);
+    }
     s.vec = reinterpret_cast<double*>(base + L.offVec);
     double* sp = reinterpret_cast<double*>(base + L.offSp);
-    s.C = sp; s.B = sp + M.ns; s.Cp = sp + 2 * M.ns; s.Ha = sp + 3 * M.ns;
-    s.dBdT = sp + 4 * M.ns; s.dCpdT = sp + 5 * M.ns;
+    s.C = sp; s.B = sp + M.ns; s.Binv = sp + 2 * M.ns; s.Cp = sp + 3 * M.ns; s.Ha = sp + 4 * M.ns;
+    s.dBdT = sp + 5 * M.ns; s.dCpdT = sp + 6 * M.ns;
     s.invD = reinterpret_cast<double*>(base + L.offInvD);
+    s.dr = reinterpret_cast<double*>(base + L.offScale);
+    s.dc = s.dr + M.n;
     s.piv = reinterpret_cast<int*>(base + L.offPiv);
     double* rx = reinterpret_cast<double*>(base + L.offRx);
     s.Kf = rx; s.Kr = rx + M.nr; s.q = rx + 2 * M.nr; s.dqdT = rx + 3 * M.nr;
@@ -225,6 +242,81 @@ __device__ __forceinline__ double clampT(const DevMech& M, double T) {
 }
 
 // ------------------------------------------------------------------------
+// exp(x) in FP64 by Tang's table-driven method (P. T. P. Tang, "Table-driven
+// implementation of the exponential function in IEEE floating-point
+// arithmetic", ACM TOMS 15(2):144-157, 1989), with 64 table entries:
+//   x = (64 m + j) ln2/64 + r,  |r| <= ln2/128,
+//   exp(x) = 2^m * 2^(j/64) * (1 + p(r)),  p(r) = r + r^2/2! + ... + r^5/5!
+// (truncation below 4e-17).  N = 64 m + j is rounded with the 1.5*2^52
+// shift, ln2/64 is split in a 36-bit head and a tail so N*head is exact, and
+// 2^m is applied by adding m to the exponent field on the integer pipe.
+// |x| > 707 (outside the range where 2^m stays a normal number) goes to the
+// CUDA exp.  About 12 FP64 instructions.
+__device__ const double kExp2Table[64] = {
+    1.0, 1.0108892860517005, 1.0218971486541166, 1.0330248790212284,
+    1.0442737824274138, 1.0556451783605572, 1.0671404006768237, 1.0787607977571199,
+    1.0905077326652577, 1.102382583307841, 1.1143867425958924, 1.1265216186082418,
+    1.1387886347566916, 1.1511892299529827, 1.1637248587775775, 1.1763969916502812,
+    1.189207115002721, 1.202156731452703, 1.215247359980469, 1.22848053610687,
+    1.241857812073484, 1.255380757024691, 1.2690509571917332, 1.2828700160787783,
+    1.2968395546510096, 1.3109612115247644, 1.3252366431597413, 1.339667524053303,
+    1.3542555469368927, 1.3690024229745905, 1.383909881963832, 1.3989796725383112,
+    1.4142135623730951, 1.42961333839197, 1.4451808069770467, 1.460917794180647,
+    1.4768261459394993, 1.4929077282912648, 1.5091644275934228, 1.5255981507445384,
+    1.5422108254079407, 1.559004400237837, 1.5759808451078865, 1.593142151342267,
+    1.6104903319492543, 1.6280274218573478, 1.645755478153965, 1.6636765803267364,
+    1.681792830507429, 1.7001063537185235, 1.718619298122478, 1.7373338352737062,
+    1.7562521603732995, 1.7753764925265212, 1.7947090750031072, 1.8142521755003989,
+    1.8340080864093424, 1.8539791250833855, 1.8741676341103, 1.8945759815869656,
+    1.9152065613971474, 1.9360617934922943, 1.9571441241754002, 1.978456026387951};
+
+__device__ __forceinline__ double fast_exp(double x) {
+    if (!(fabs(x) <= 707.0)) return exp(x);
+    const double kInvL = 92.33248261689366;          // 64/ln2
+    const double kL1 = 0.010830424696223417;         // head of ln2/64 (36 bits)
+    const double kL2 = 2.572804622327669e-14;        // tail
+    const double kShift = 6755399441055744.0;        // 1.5 * 2^52
+    const double kk = fma(x, kInvL, kShift);
+    const long long N = __double_as_longlong(kk) - 0x4338000000000000LL;
+    const double Nf = kk - kShift;
+    double r = fma(-Nf, kL1, x);
+    r = fma(-Nf, kL2, r);
+    double q = fma(r, 1.0 / 120.0, 1.0 / 24.0);
+    q = fma(r, q, 1.0 / 6.0);
+    q = fma(r, q, 0.5);
+    q = fma(r, q, 1.0);
+    const double p = r * q;
+    const double S = __ldg(&kExp2Table[N & 63]);
+    const double res = fma(S, p, S);
+    return __longlong_as_double(__double_as_longlong(res) + ((N >> 6) << 52));
+}
+
+// (Pstd/(Ru T))^(-dnu) for dnu = -2..2: the pressure factor of 1/Kc
+struct PFactor { double v[5]; };
+
+__device__ __forceinline__ PFactor pressure_factors(double Tc) {
+    const double invPByRT = kRu * Tc / kPstd;
+    const double PByRT = 1.0 / invPByRT;
+    PFactor f;
+    f.v[0] = PByRT * PByRT; f.v[1] = PByRT; f.v[2] = 1.0; f.v[3] = invPByRT; f.v[4] = invPByRT * invPByRT;
+    return f;
+}
+
+constexpr double kInvKcClamp = 1.0 / kKcClamp;
+
+// 1/Kc from per-species exp(-G/RT) and its inverse, no division:
+// 1/Kc = prod_reactants E * prod_products 1/E * (Pstd/(Ru T))^-dnu, with the
+// reference's lower clamp of Kc (ReactionFunctionI.H:17) as an upper clamp.
+__device__ __forceinline__ double inv_equilibrium_kc(const RxnInfo& x, const double* E, const double* Einv,
+                                                     const PFactor& pf) {
+    double v = E[x.sl[0]];
+    for (int q = 1; q < x.nl; q++) v *= E[x.sl[q]];
+    for (int q = 0; q < x.nr; q++) v *= Einv[x.sr[q]];
+    if (x.dnu != 0) v *= pf.v[x.dnu + 2];
+    return v > kInvKcClamp ? kInvKcClamp : v;
+}
+
+// ------------------------------------------------------------------------
 // rate constants
 
 // PLOG: ln k linear in ln p between the bracketing rows, clamped to the end
@@ -258,27 +350,9 @@ __device__ __forceinline__ double plog_rate(const DevMech& M, int ip, double p, 
         lk = laa + ba * logT - ta * invT + ((lab - laa) + (bb - ba) * logT - (tb - ta) * invT) * fr;
         dk = invT * (ba + ta * invT + (bb - ba + (tb - ta) * invT) * fr);
     }
-    const double k = exp(lk);
+    const double k = fast_exp(lk);
     *dkdT = k * dk;
     return k;
-}
-
-// Kc = Kp (Pstd/(Ru T))^dnu clamped from below (ReactionFunctionI.H RF11..RF33,
-// ChemicalEquilibriumFunctionI.H:14-25)
-__device__ __forceinline__ double equilibrium_kc(const RxnInfo& x, const double* B, double PByRT) {
-    double num = B[x.sr[0]];
-    for (int q = 1; q < x.nr; q++) num *= B[x.sr[q]];
-    double den = B[x.sl[0]];
-    for (int q = 1; q < x.nl; q++) den *= B[x.sl[q]];
-    double Kc = num / den;
-    switch (x.dnu) {
-        case -2: Kc = Kc * (1 / (PByRT * PByRT)); break;
-        case -1: Kc = Kc * (1 / PByRT); break;
-        case 1: Kc = Kc * PByRT; break;
-        case 2: Kc = Kc * (PByRT * PByRT); break;
-        default: break;
-    }
-    return Kc > kKcClamp ? Kc : kKcClamp;
 }
 
 __device__ __forceinline__ RxnInfo load_rx(const RxnInfo* p) {
@@ -320,7 +394,9 @@ __device__ __noinline__ void rhs_eval(const Grp<G>& g, const DevMech& M, const S
         const double invW = __ldg(&M.invW[i]);
         s.C[i] = rhoM * invW * YT[i];
         const Nasa a = load_nasa(species_coeffs(M, i, Tc));
-        s.B[i] = exp(gibbs_exponent(a, Tc, invT, logT));
+        const double Ei = fast_exp(gibbs_exponent(a, Tc, invT, logT));
+        s.B[i] = Ei;
+        s.Binv[i] = 1.0 / Ei;
         const double RuInvW = invW * kRu;
         s.Cp[i] = cp_of(a, Tp, RuInvW);
         s.Ha[i] = ha_of(a, Tp, RuInvW);
@@ -333,7 +409,7 @@ __device__ __noinline__ void rhs_eval(const Grp<G>& g, const DevMech& M, const S
         s.Mtb[t] = m;
     }
     g.sync();
-    const double PByRT = kPstd / (kRu * Tc);
+    const PFactor pf = pressure_factors(Tc);
     const double logP = M.nPlog ? log(p) : 0.0;
     for (int r = g.rank; r < M.nr; r += G) {
         const RxnInfo x = load_rx(M.rx + r);
@@ -344,11 +420,11 @@ __device__ __noinline__ void rhs_eval(const Grp<G>& g, const DevMech& M, const S
         } else if (x.tind) {
             Kf = x.A;
         } else {
-            Kf = x.A * exp(fma(x.beta, logT, -(x.Ta * invT)));
+            Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
         }
         if (x.tb >= 0) Kf *= s.Mtb[x.tb];
         double Kr = 0;
-        if (x.rev) Kr = Kf / equilibrium_kc(x, s.B, PByRT);
+        if (x.rev) Kr = Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
         double CF = s.C[x.sl[0]];
         for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
         double CR = s.C[x.sr[0]];
@@ -389,7 +465,9 @@ __device__ __noinline__ double rates_eval(const Grp<G>& g, const DevMech& M, con
     for (int i = g.rank; i < ns; i += G) {
         s.C[i] = rho * Y[i] / __ldg(&M.W[i]);
         const Nasa a = load_nasa(species_coeffs(M, i, Tc));
-        s.B[i] = exp(gibbs_exponent(a, Tc, invT, logT));
+        const double Ei = fast_exp(gibbs_exponent(a, Tc, invT, logT));
+        s.B[i] = Ei;
+        s.Binv[i] = 1.0 / Ei;
     }
     g.sync();
     for (int t = g.rank; t < M.nTB; t += G) {
@@ -399,7 +477,7 @@ __device__ __noinline__ double rates_eval(const Grp<G>& g, const DevMech& M, con
         s.Mtb[t] = m;
     }
     g.sync();
-    const double PByRT = kPstd / (kRu * Tc);
+    const PFactor pf = pressure_factors(Tc);
     const double logP = M.nPlog ? log(p) : 0.0;
     for (int r = g.rank; r < M.nr; r += G) {
         const RxnInfo x = load_rx(M.rx + r);
@@ -410,11 +488,11 @@ __device__ __noinline__ double rates_eval(const Grp<G>& g, const DevMech& M, con
         } else if (x.tind) {
             Kf = x.A;
         } else {
-            Kf = x.A * exp(fma(x.beta, logT, -(x.Ta * invT)));
+            Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
         }
         if (x.tb >= 0) Kf *= s.Mtb[x.tb];
         double Kr = 0;
-        if (x.rev) Kr = Kf / equilibrium_kc(x, s.B, PByRT);
+        if (x.rev) Kr = Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
         double CF = s.C[x.sl[0]];
         for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
         double CR = s.C[x.sr[0]];
@@ -475,7 +553,9 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
         const double y = YT[i], invW = __ldg(&M.invW[i]);
         const Nasa a = load_nasa(species_coeffs(M, i, Tc));
         s.C[i] = rhoM * y * invW;
-        s.B[i] = exp(gibbs_exponent(a, Tc, invT, logT));
+        const double Ei = fast_exp(gibbs_exponent(a, Tc, invT, logT));
+        s.B[i] = Ei;
+        s.Binv[i] = 1.0 / Ei;
         s.dBdT[i] = fma(fma(a.a5, invT, a.a0), invT,
                         fma(fma(fma(a.a4 * 0.2, Tc, a.a3 * 0.25), Tc, a.a2 * (1.0 / 3.0)), Tc, a.a1 * 0.5));
         const double RuInvW = invW * kRu;
@@ -498,7 +578,7 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
     }
     g.sync();
     // per-reaction rate constants, their temperature derivatives and q
-    const double PByRT = kPstd / (kRu * Tc);
+    const PFactor pf = pressure_factors(Tc);
     const double logP = M.nPlog ? log(p) : 0.0;
     for (int r = g.rank; r < M.nr; r += G) {
         const RxnInfo x = load_rx(M.rx + r);
@@ -508,7 +588,7 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
         } else if (x.tind) {
             Kf = x.A; dKfdT = 0;
         } else {
-            Kf = x.A * exp(fma(x.beta, logT, -(x.Ta * invT)));
+            Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
             dKfdT = Kf * (fma(x.Ta, invT, x.beta) * invT);
         }
         double dKfdC = 0;
@@ -520,15 +600,15 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
         }
         double Kr = 0, dKrdT = 0, invKc = 0;
         if (x.rev) {
-            const double Kc = equilibrium_kc(x, s.B, PByRT);
+            invKc = inv_equilibrium_kc(x, s.B, s.Binv, pf);
             double sv = s.dBdT[x.sr[0]];
             for (int q = 1; q < x.nr; q++) sv += s.dBdT[x.sr[q]];
             double sl = s.dBdT[x.sl[0]];
             for (int q = 1; q < x.nl; q++) sl += s.dBdT[x.sl[q]];
             const double dKcdTByKc = (sv - sl) - x.dnu * invT;
-            invKc = 1.0 / Kc;
             Kr = Kf * invKc;
-            dKrdT = dKfdT * invKc - (Kc > kKcClamp ? Kr * dKcdTByKc : 0.0);
+            // the Kc term of dKr/dT is dropped when Kc sits on its clamp (JacobianFunctionI.H:246-249)
+            dKrdT = dKfdT * invKc - (invKc < kInvKcClamp ? Kr * dKcdTByKc : 0.0);
         }
         double CF = s.C[x.sl[0]];
         for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
@@ -538,73 +618,86 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
         s.Kr[r] = Kr;
         s.q[r] = Kf * CF - Kr * CR;
         s.dqdT[r] = dKfdT * CF - dKrdT * CR;
-        if (x.tb >= 0) {
-            s.tbF[x.tb] = dKfdC;
-            s.tbR[x.tb] = dKfdC * invKc;
-            s.tbCF[x.tb] = CF;
-            s.tbCR[x.tb] = CR;
-        }
+        // third-body weight w = dKf/dM CF - dKr/dM CR, dKr/dM = dKf/dM / Kc
+        if (x.tb >= 0) s.tbF[x.tb] = dKfdC * CF - (dKfdC * invKc) * CR;
     }
+    for (int idx = g.rank; idx < ns * ld; idx += G) J[idx] = MT(0);
     g.sync();
-    // Row owners gather the concentration Jacobian of their species row in
-    // reaction order, then convert the row to the mass-fraction Jacobian.
-    double dtd = 0, dd = 0;
-    for (int i = g.rank; i < ns; i += G) {
-        MT* row = J + (size_t)i * ld;
-        for (int j = 0; j < n; j++) row[j] = MT(0);
-        double w = 0;
-        const int e1 = __ldg(&M.incOff[i + 1]);
-        for (int e = __ldg(&M.incOff[i]); e < e1; e++) {
+    // (1) column owners: d q_r / d C_j computed once per (reaction, column)
+    // occurrence and scattered down column j to the rows of reaction r, in
+    // reaction order (JF11..JF33 reverse and forward concentration terms).
+    for (int j = g.rank; j < ns; j += G) {
+        const int e1 = __ldg(&M.incOff[j + 1]);
+        for (int e = __ldg(&M.incOff[j]); e < e1; e++) {
             const int v = __ldg(&M.inc[e]);
             const int r = v >> 1;
             const bool prod = v & 1;
             const RxnInfo x = load_rx(M.rx + r);
-            const double Kf = s.Kf[r], Kr = s.Kr[r];
-            if (x.rev) {
-                for (int pp = 0; pp < x.nr; pp++) {
-                    double d = 1.0;
-                    for (int qq = 0; qq < x.nr; qq++) if (qq != pp) d *= s.C[x.sr[qq]];
-                    const double val = -Kr * d;
-                    const int col = x.sr[pp];
-                    row[col] = prod ? row[col] + MT(val) : row[col] - MT(val);
+            double d;
+            if (!prod) {
+                // forward: Kf * product of the other reactant concentrations
+                bool skipped = false;
+                d = s.Kf[r];
+                for (int q = 0; q < x.nl; q++) {
+                    if (!skipped && x.sl[q] == j) { skipped = true; continue; }
+                    d *= s.C[x.sl[q]];
+                }
+            } else {
+                if (!x.rev) continue;
+                bool skipped = false;
+                d = -s.Kr[r];
+                for (int q = 0; q < x.nr; q++) {
+                    if (!skipped && x.sr[q] == j) { skipped = true; continue; }
+                    d *= s.C[x.sr[q]];
                 }
             }
-            const double qq = s.q[r];
-            w = prod ? w + qq : w - qq;
-            row[ns] = prod ? row[ns] + MT(s.dqdT[r]) : row[ns] - MT(s.dqdT[r]);
-            for (int pp = 0; pp < x.nl; pp++) {
-                double d = 1.0;
-                for (int q2 = 0; q2 < x.nl; q2++) if (q2 != pp) d *= s.C[x.sl[q2]];
-                const double val = Kf * d;
-                const int col = x.sl[pp];
-                row[col] = prod ? row[col] + MT(val) : row[col] - MT(val);
-            }
-            if (x.tb >= 0) {
-                const double dF = s.tbF[x.tb], dR = s.tbR[x.tb];
-                const double CF = s.tbCF[x.tb], CR = s.tbCR[x.tb];
-                const double* eff = M.eff + (size_t)x.tb * ns;
-                for (int j = 0; j < ns; j++) {
-                    const double ej = __ldg(&eff[j]);
-                    const double Wd = (dF * ej) * CF - (dR * ej) * CR;
-                    row[j] = prod ? row[j] + MT(Wd) : row[j] - MT(Wd);
-                }
-            }
+            const MT md = MT(d);
+            for (int q = 0; q < x.nl; q++) { MT& c = J[(size_t)x.sl[q] * ld + j]; c = c - md; }
+            for (int q = 0; q < x.nr; q++) { MT& c = J[(size_t)x.sr[q] * ld + j]; c = c + md; }
+        }
+    }
+    g.sync();
+    // (2) third-body columns, J_ij += nu_i w_t E_tj (JF* third-body block)
+    for (int j = g.rank; j < ns; j += G) {
+        for (int e = 0; e < M.nTbInc; e++) {
+            const int v = __ldg(&M.tbInc[e]);
+            const int i = v >> 16, t = (v >> 1) & 0x7fff;
+            const double wd = __ldg(&M.eff[(size_t)t * ns + j]) * s.tbF[t];
+            MT& c = J[(size_t)i * ld + j];
+            c = (v & 1) ? c + MT(wd) : c - MT(wd);
+        }
+    }
+    g.sync();
+    // (3) row owners: production rate and temperature column by gather, then
+    // the dC/dY conversion of the row (diagonal scaling + rank-1 correction)
+    double dtd = 0, dd = 0;
+    for (int i = g.rank; i < ns; i += G) {
+        MT* row = J + (size_t)i * ld;
+        double w = 0, tc = 0;
+        const int e1 = __ldg(&M.incOff[i + 1]);
+        for (int e = __ldg(&M.incOff[i]); e < e1; e++) {
+            const int v = __ldg(&M.inc[e]);
+            const int r = v >> 1;
+            const double qq = s.q[r], dq = s.dqdT[r];
+            if (v & 1) { w += qq; tc += dq; } else { w -= qq; tc -= dq; }
         }
         const double WiByrhoM = invRhoM * __ldg(&M.W[i]);
         const double dY = w * WiByrhoM;
         double S = 0;
         for (int k = 0; k < ns; k++) S = fma(double(row[k]), s.C[k], S);
-        const double tcol = WiByrhoM * (double(row[ns]) - S * invT) + invT * dY;
+        const double tcol = WiByrhoM * (tc - S * invT) + invT * dY;
         if (fast) {
             for (int j = 0; j < ns; j++) {
-                const double mj = MW * __ldg(&M.invW[j]);
-                row[j] = MT(WiByrhoM * (double(row[j]) * (rhoM * __ldg(&M.invW[j]))) + mj * dY);
+                const double invWj = __ldg(&M.invW[j]);
+                row[j] = MT(WiByrhoM * (double(row[j]) * (rhoM * invWj)) + (MW * invWj) * dY);
             }
         } else {
+            // Wi/rho (Jc_ij rho/Wj - m_j S) + m_j dY = Jc_ij (Wi/Wj) + m_j (dY - Wi/rho S)
+            const double K = dY - WiByrhoM * S;
+            const double Wi = __ldg(&M.W[i]);
             for (int j = 0; j < ns; j++) {
                 const double invWj = __ldg(&M.invW[j]);
-                const double mj = MW * invWj;
-                row[j] = MT(WiByrhoM * fma(double(row[j]), rhoM * invWj, -(mj * S)) + mj * dY);
+                row[j] = MT(fma(double(row[j]), Wi * invWj, (MW * invWj) * K));
             }
         }
         row[ns] = MT(tcol);
@@ -697,78 +790,58 @@ __device__ __noinline__ void lu_factor(const Grp<G>& g, MT* A, int n, int ld, in
         }
         g.sync();
     }
+    // The interchange sequence as one gather permutation (P b)[i] = b[perm[i]]
+    // for the solves, written over piv.
+    if (g.rank == 0) {
+        int perm[256];
+        for (int i = 0; i < n; i++) perm[i] = i;
+        for (int j = 0; j < n; j++) {
+            const int pj = piv[j];
+            if (pj != j) { const int t = perm[j]; perm[j] = perm[pj]; perm[pj] = t; }
+        }
+        for (int i = 0; i < n; i++) piv[i] = perm[i];
+    }
+    g.sync();
 }
 
-// Forward/back substitution with the factors of lu_factor, applying the row
-// interchanges first (LUsolver.C:3145-3171, 4113-4152).  b is a shared-slot
-// vector of doubles; arithmetic in MT.
+// Forward/back substitution with the factors of lu_factor after the row
+// interchanges (LUsolver.C:3145-3171, 4113-4152).  One warp of the group
+// does the column sweeps (shared-memory vector, one __syncwarp per column);
+// the other warps wait at the closing group barrier.  b is a slot vector of
+// doubles; arithmetic in MT.
 template<int G, class MT>
-__device__ __noinline__ void lu_solve(const Grp<G>& g, const MT* A, int n, int ld, const int* piv,
-                         const double* invD, double* b) {
-    if constexpr (G == 32) {
-        constexpr int NR = 8;  // up to 256 unknowns in registers
+__device__ __noinline__ void lu_solve(const Grp<G>& g, const MT* A, int n, int ld, const int* perm,
+                                      const double* invD, double* b) {
+    g.sync();
+    if (g.rank < 32) {
         const int lane = g.rank;
-        __syncwarp();
-        if (lane == 0) {
-            for (int j = 0; j < n; j++) {
-                const int pj = piv[j];
-                if (pj != j) { const double t = b[pj]; b[pj] = b[j]; b[j] = t; }
-            }
-        }
-        __syncwarp();
-        MT x[NR];
+        double t[8];
 #pragma unroll
-        for (int u = 0; u < NR; u++) {
+        for (int u = 0; u < 8; u++) {
             const int i = lane + 32 * u;
-            x[u] = i < n ? MT(b[i]) : MT(0);
+            t[u] = i < n ? b[perm[i]] : 0.0;
         }
-        for (int j = 0; j < n - 1; j++) {
-            const MT bj = __shfl_sync(0xffffffffu, x[j >> 5], j & 31);
+        __syncwarp();
 #pragma unroll
-            for (int u = 0; u < NR; u++) {
-                const int i = lane + 32 * u;
-                if (i > j && i < n) x[u] = fma(-A[(size_t)i * ld + j], bj, x[u]);
-            }
+        for (int u = 0; u < 8; u++) {
+            const int i = lane + 32 * u;
+            if (i < n) b[i] = t[u];
+        }
+        __syncwarp();
+        for (int j = 0; j < n - 1; j++) {
+            const MT bj = MT(b[j]);
+            for (int i = j + 1 + lane; i < n; i += 32) b[i] = double(fma(-A[(size_t)i * ld + j], bj, MT(b[i])));
+            __syncwarp();
         }
         for (int j = n - 1; j >= 0; j--) {
-            const MT xj = __shfl_sync(0xffffffffu, x[j >> 5], j & 31) * MT(invD[j]);
-#pragma unroll
-            for (int u = 0; u < NR; u++) {
-                const int i = lane + 32 * u;
-                if (i == j) x[u] = xj;
-                else if (i < j) x[u] = fma(-A[(size_t)i * ld + j], xj, x[u]);
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < NR; u++) {
-            const int i = lane + 32 * u;
-            if (i < n) b[i] = double(x[u]);
+            const MT xj = MT(b[j]) * MT(invD[j]);
+            for (int i = lane; i < j; i += 32) b[i] = double(fma(-A[(size_t)i * ld + j], xj, MT(b[i])));
+            __syncwarp();
+            if (lane == (j & 31)) b[j] = double(xj);
         }
         __syncwarp();
-    } else {
-        g.sync();
-        if (g.rank == 0) {
-            for (int j = 0; j < n; j++) {
-                const int pj = piv[j];
-                if (pj != j) { const double t = b[pj]; b[pj] = b[j]; b[j] = t; }
-            }
-        }
-        g.sync();
-        for (int j = 0; j < n - 1; j++) {
-            const double bj = b[j];
-            for (int i = j + 1 + g.rank; i < n; i += G)
-                b[i] = double(fma(-A[(size_t)i * ld + j], MT(bj), MT(b[i])));
-            g.sync();
-        }
-        for (int j = n - 1; j >= 0; j--) {
-            const double xj = double(MT(b[j]) * MT(invD[j]));
-            for (int i = g.rank; i < j; i += G)
-                b[i] = double(fma(-A[(size_t)i * ld + j], MT(xj), MT(b[i])));
-            g.sync();
-            if (g.rank == 0) b[j] = xj;
-            g.sync();
-        }
     }
+    g.sync();
 }
 
 }  // namespace fcs

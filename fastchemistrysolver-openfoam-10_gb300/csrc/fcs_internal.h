@@ -54,6 +54,8 @@ struct DevMech {
     const double* plogTa;   // [rows]
     const int* incOff;      // [ns+1]
     const int* inc;         // (reaction << 1) | (1 if product else 0)
+    int nTbInc;             // third-body incidences (species row, third-body row, side)
+    const int* tbInc;       // (row << 16) | (tb << 1) | (1 if product else 0), reaction order
     const double* hf;       // [ns] formation enthalpy at 298.15 K, J/kg (for Qdot)
 };
 
@@ -70,6 +72,6 @@ struct KOpts {
 
 // Per-cell status / counters layout in the stats buffer (int64 each).
 enum { ST_CELLS = 0, ST_SKIPPED, ST_FAILED, ST_ATTEMPTS, ST_ACCEPTED, ST_JAC, ST_LU,
-       ST_RHS, ST_SOLVES, ST_COUNT };
+       ST_RHS, ST_SOLVES, ST_FALLBACK, ST_COUNT };
 
 }  // namespace fcs

@@ -23,50 +23,160 @@
 namespace fcs {
 
 // ------------------------------------------------------------------------
-// linear solves used by the integrators
+// linear algebra of one attempt
 
-// FP64 method: the LU factors are the FP64 matrix itself.
-// Mixed method: x = LU32^-1 b, r = b - A x with A = c I - J formed on the fly
-// from the kept FP32 Jacobian in FP64 arithmetic, x += LU32^-1 r.
-template<int G, class MT>
-__device__ __noinline__ void linear_solve(const Grp<G>& g, const DevMech& M, const Slot<MT>& s, double c,
-                             double* b, double* tmp) {
-    const int n = M.n, ld = s.ld;
-    if constexpr (sizeof(MT) == 8) {
-        lu_solve<G, MT>(g, s.LU, n, ld, s.piv, s.invD, b);
-    } else {
-        for (int i = g.rank; i < n; i += G) tmp[i] = b[i];
-        lu_solve<G, MT>(g, s.LU, n, ld, s.piv, s.invD, b);   // b <- x0 (also synced)
-        for (int i = g.rank; i < n; i += G) {
-            const MT* Ji = s.J + (size_t)i * ld;
-            double r = tmp[i] - c * b[i];
-            for (int j = 0; j < n; j++) r = fma(double(Ji[j]), b[j], r);
-            tmp[i] = r;
+struct CellCounters {
+    long long attempts = 0, accepted = 0, jac = 0, lu = 0, rhs = 0, solves = 0, fallbacks = 0;
+};
+
+// Accepted size of the refinement correction relative to the solution
+// (max norm); above it the FP32 factorisation is not trusted for this matrix
+// and the attempt is redone in FP64.
+constexpr double kRefineTol = 1e-3;
+
+// FP64 Jacobian (assembled in the FP64 view of the matrix region) -> FP32
+// Jacobian at the start of the same region.  Rounds of G*R elements: every
+// element a round overwrites (bytes [4k, 4k+4)) was read in this or an
+// earlier round, so the in-place narrowing is race free.
+template<int G>
+__device__ __noinline__ void jac_to_fp32(const Grp<G>& g, const double* J64, float* J32, int count) {
+    constexpr int R = 4;
+    for (int start = 0; start < count; start += G * R) {
+        double v[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int k = start + r * G + g.rank;
+            v[r] = k < count ? J64[k] : 0.0;
         }
         g.sync();
-        // correction solve on the residual, written into tmp
-        lu_solve<G, MT>(g, s.LU, n, ld, s.piv, s.invD, tmp);
-        for (int i = g.rank; i < n; i += G) b[i] += tmp[i];
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int k = start + r * G + g.rank;
+            if (k < count) J32[k] = float(v[r]);
+        }
         g.sync();
     }
 }
 
-// A = c I - J into the LU slot (in place for the FP64 single-matrix layout)
-template<int G, class MT>
-__device__ __noinline__ void form_iteration_matrix(const Grp<G>& g, const Slot<MT>& s, int n, double c) {
+// FP64: A = c I - J into the LU view (in place for the single-matrix layout)
+template<int G>
+__device__ __noinline__ void form_iteration_matrix(const Grp<G>& g, const Slot<double>& s, int n, double c) {
     const int ld = s.ld;
     for (int idx = g.rank; idx < n * ld; idx += G) {
         const int i = idx / ld, j = idx - i * ld;
         if (j >= n) continue;
-        const MT v = -s.J[idx];
-        s.LU[idx] = (i == j) ? MT(double(v) + c) : v;
+        const double v = -s.J[idx];
+        s.LU[idx] = (i == j) ? v + c : v;
     }
     g.sync();
 }
 
-struct CellCounters {
-    long long attempts = 0, accepted = 0, jac = 0, lu = 0, rhs = 0, solves = 0;
-};
+__device__ __forceinline__ double pow2_inverse(float m) {
+    // 2^-e with e the binary exponent of m (exact scaling); 1 for 0/inf/nan
+    if (!(m > 0.f) || !(m < 3.0e38f)) return 1.0;
+    return ldexp(1.0, -ilogbf(m));
+}
+
+// Mixed: LU32 = Dr (c I - J32) Dc with power-of-two row and column
+// equilibration (Dr, Dc kept in s.dr / s.dc for the solves).
+template<int G>
+__device__ __noinline__ void form_iteration_matrix_scaled(const Grp<G>& g, const Slot<float>& s, int n,
+                                                          double c) {
+    const int ld = s.ld;
+    for (int i = g.rank; i < n; i += G) {
+        const float* row = s.J + (size_t)i * ld;
+        float mx = 0.f;
+        for (int j = 0; j < n; j++) {
+            const float a = (i == j) ? float(c - double(row[j])) : -row[j];
+            mx = fmaxf(mx, fabsf(a));
+        }
+        s.dr[i] = pow2_inverse(mx);
+    }
+    g.sync();
+    for (int j = g.rank; j < n; j += G) {
+        float mx = 0.f;
+        for (int i = 0; i < n; i++) {
+            const float jv = s.J[(size_t)i * ld + j];
+            const float a = (i == j) ? float(c - double(jv)) : -jv;
+            mx = fmaxf(mx, fabsf(a * float(s.dr[i])));
+        }
+        s.dc[j] = pow2_inverse(mx);
+    }
+    g.sync();
+    for (int idx = g.rank; idx < n * ld; idx += G) {
+        const int i = idx / ld, j = idx - i * ld;
+        if (j >= n) continue;
+        const float jv = s.J[idx];
+        const float a = (i == j) ? float(c - double(jv)) : -jv;
+        s.LU[idx] = a * float(s.dr[i]) * float(s.dc[j]);
+    }
+    g.sync();
+}
+
+// Mixed solve: x0 = Dc LU32^-1 Dr b (FP32), r = b - (c x0 - J32 x0) in FP64,
+// x = x0 + Dc LU32^-1 Dr r.  Returns false when the correction is not small
+// (or not finite): the caller then repeats the work in FP64.
+template<int G>
+__device__ __noinline__ bool linear_solve_mixed(const Grp<G>& g, const DevMech& M, const Slot<float>& s,
+                                                double c, double* b, double* tmp) {
+    const int n = M.n, ld = s.ld;
+    for (int i = g.rank; i < n; i += G) {
+        tmp[i] = b[i];
+        b[i] = b[i] * s.dr[i];
+    }
+    g.sync();
+    lu_solve<G, float>(g, s.LU, n, ld, s.piv, s.invD, b);
+    for (int i = g.rank; i < n; i += G) b[i] = b[i] * s.dc[i];
+    g.sync();
+    for (int i = g.rank; i < n; i += G) {
+        const float* Ji = s.J + (size_t)i * ld;
+        double r = tmp[i] - c * b[i];
+        for (int j = 0; j < n; j++) r = fma(double(Ji[j]), b[j], r);
+        tmp[i] = r * s.dr[i];
+    }
+    g.sync();
+    lu_solve<G, float>(g, s.LU, n, ld, s.piv, s.invD, tmp);
+    double dmax = 0, xmax = 0;
+    for (int i = g.rank; i < n; i += G) {
+        const double d = tmp[i] * s.dc[i];
+        const double x = b[i] + d;
+        b[i] = x;
+        const double ad = fabs(d), ax = fabs(x);
+        dmax = (ad > dmax || ad != ad) ? ad : dmax;
+        xmax = (ax > xmax || ax != ax) ? ax : xmax;
+    }
+    dmax = gmax(g, dmax, s.red);
+    xmax = gmax(g, xmax, s.red);
+    g.sync();
+    return dmax <= kRefineTol * xmax && xmax < 1e300;
+}
+
+// Jacobian of the attempt: assembled in FP64 (cancellation between fast
+// forward and reverse terms needs it), kept in FP32 in mixed precision.
+template<int G, class MT>
+__device__ __forceinline__ void jacobian_into(const Grp<G>& g, const DevMech& M, const Slot<MT>& s,
+                                              const Slot<double>& sd, double p, double* y, double* f, int fast) {
+    jac_eval<G, double>(g, M, sd, p, y, f, sd.J, fast);
+    if constexpr (sizeof(MT) == 4) jac_to_fp32<G>(g, sd.J, s.J, M.n * s.ld);
+}
+
+template<int G, class MT>
+__device__ __forceinline__ void factor_iteration(const Grp<G>& g, const DevMech& M, const Slot<MT>& s, double c) {
+    if constexpr (sizeof(MT) == 8) form_iteration_matrix<G>(g, s, M.n, c);
+    else form_iteration_matrix_scaled<G>(g, s, M.n, c);
+    lu_factor<G, MT>(g, s.LU, M.n, s.ld, s.piv, s.invD);
+}
+
+template<int G, class MT>
+__device__ __forceinline__ bool stage_solve(const Grp<G>& g, const DevMech& M, const Slot<MT>& s, double c,
+                                            double* b, double* tmp) {
+    if constexpr (sizeof(MT) == 8) {
+        lu_solve<G, double>(g, s.LU, M.n, s.ld, s.piv, s.invD, b);
+        return true;
+    } else {
+        return linear_solve_mixed<G>(g, M, s, c, b, tmp);
+    }
+}
 
 // ------------------------------------------------------------------------
 // Rosenbrock attempts
@@ -75,8 +185,8 @@ struct CellCounters {
 // Vectors: 0 y0, 1 yTemp, 2..6 k1..k5, 7 dy, 8 err, 9 dydx, 10 dfdx, 11 tmp
 template<int G, class MT>
 __device__ __noinline__ double rodas34_attempt(const Grp<G>& g, const DevMech& M, const KOpts& o,
-                                  const Slot<MT>& s, double p, double dx, double invdx,
-                                  CellCounters& cc) {
+                                  const Slot<MT>& s, const Slot<double>& sd, double p, double dx,
+                                  double invdx, CellCounters& cc) {
     const int n = M.n;
     double *y0 = s.v(0), *yTemp = s.v(1), *k1 = s.v(2), *k2 = s.v(3), *k3 = s.v(4), *k4 = s.v(5);
     double *k5 = s.v(6), *dy = s.v(7), *err = s.v(8), *dydx = s.v(9), *dfdx = s.v(10), *tmp = s.v(11);
@@ -93,16 +203,15 @@ __device__ __noinline__ double rodas34_attempt(const Grp<G>& g, const DevMech& M
                  c64 = 0.1631930543123136e2, c65 = -0.6058818238834054e1;
     const double invgamma = 1.0 / 0.25;
 
-    jac_eval<G, MT>(g, M, s, p, y0, dfdx, s.J, o.jacobian);
+    jacobian_into<G, MT>(g, M, s, sd, p, y0, dfdx, o.jacobian);
     const double cdiag = 1.0 * invdx * invgamma;
-    form_iteration_matrix<G, MT>(g, s, n, cdiag);
-    lu_factor<G, MT>(g, s.LU, n, s.ld, s.piv, s.invD);
+    factor_iteration<G, MT>(g, M, s, cdiag);
     cc.jac++; cc.lu++; cc.rhs += 5; cc.solves += 6;
 
     const double dxd1 = dx * d1 + 1;
     for (int i = g.rank; i < n; i += G) k1[i] = dxd1 * dfdx[i];
     g.sync();
-    linear_solve<G, MT>(g, M, s, cdiag, k1, tmp);
+    if (!stage_solve<G, MT>(g, M, s, cdiag, k1, tmp)) return -1.0;
     for (int i = g.rank; i < n; i += G) yTemp[i] = fma(a21, k1[i], y0[i]);
     g.sync();
     rhs_eval<G, MT>(g, M, s, p, yTemp, dydx, 1);
@@ -111,7 +220,7 @@ __device__ __noinline__ double rodas34_attempt(const Grp<G>& g, const DevMech& M
         for (int i = g.rank; i < n; i += G) k2[i] = fma(e1, k1[i], fma(dxd2, dfdx[i], dydx[i]));
     }
     g.sync();
-    linear_solve<G, MT>(g, M, s, cdiag, k2, tmp);
+    if (!stage_solve<G, MT>(g, M, s, cdiag, k2, tmp)) return -1.0;
     for (int i = g.rank; i < n; i += G) yTemp[i] = fma(a32, k2[i], fma(a31, k1[i], y0[i]));
     g.sync();
     rhs_eval<G, MT>(g, M, s, p, yTemp, dydx, 1);
@@ -120,7 +229,7 @@ __device__ __noinline__ double rodas34_attempt(const Grp<G>& g, const DevMech& M
         for (int i = g.rank; i < n; i += G) k3[i] = fma(e2, k2[i], fma(e1, k1[i], fma(dxd3, dfdx[i], dydx[i])));
     }
     g.sync();
-    linear_solve<G, MT>(g, M, s, cdiag, k3, tmp);
+    if (!stage_solve<G, MT>(g, M, s, cdiag, k3, tmp)) return -1.0;
     for (int i = g.rank; i < n; i += G) yTemp[i] = fma(a43, k3[i], fma(a42, k2[i], fma(a41, k1[i], y0[i])));
     g.sync();
     rhs_eval<G, MT>(g, M, s, p, yTemp, dydx, 1);
@@ -130,7 +239,7 @@ __device__ __noinline__ double rodas34_attempt(const Grp<G>& g, const DevMech& M
             k4[i] = fma(e3, k3[i], fma(e2, k2[i], fma(e1, k1[i], fma(dxd4, dfdx[i], dydx[i]))));
     }
     g.sync();
-    linear_solve<G, MT>(g, M, s, cdiag, k4, tmp);
+    if (!stage_solve<G, MT>(g, M, s, cdiag, k4, tmp)) return -1.0;
     for (int i = g.rank; i < n; i += G) {
         const double d = fma(a54, k4[i], fma(a53, k3[i], fma(a52, k2[i], a51 * k1[i])));
         dy[i] = d;
@@ -144,7 +253,7 @@ __device__ __noinline__ double rodas34_attempt(const Grp<G>& g, const DevMech& M
             k5[i] = fma(e4, k4[i], fma(e3, k3[i], fma(e2, k2[i], fma(e1, k1[i], dydx[i]))));
     }
     g.sync();
-    linear_solve<G, MT>(g, M, s, cdiag, k5, tmp);
+    if (!stage_solve<G, MT>(g, M, s, cdiag, k5, tmp)) return -1.0;
     for (int i = g.rank; i < n; i += G) {
         const double d = dy[i] + k5[i];
         dy[i] = d;
@@ -158,7 +267,7 @@ __device__ __noinline__ double rodas34_attempt(const Grp<G>& g, const DevMech& M
             err[i] = fma(e5, k5[i], fma(e4, k4[i], fma(e3, k3[i], fma(e2, k2[i], fma(e1, k1[i], dydx[i])))));
     }
     g.sync();
-    linear_solve<G, MT>(g, M, s, cdiag, err, tmp);
+    if (!stage_solve<G, MT>(g, M, s, cdiag, err, tmp)) return -1.0;
     double me = 0;
     for (int i = g.rank; i < n; i += G) {
         const double yt = y0[i] + dy[i] + err[i];
@@ -173,8 +282,8 @@ __device__ __noinline__ double rodas34_attempt(const Grp<G>& g, const DevMech& M
 // OptRosenbrock34::Rosenbrock34Solve (OptRosenbrock34.C:281-678), .H:127-158
 template<int G, class MT>
 __device__ __noinline__ double ros34_attempt(const Grp<G>& g, const DevMech& M, const KOpts& o,
-                                const Slot<MT>& s, double p, double dx, double invdx,
-                                CellCounters& cc) {
+                                const Slot<MT>& s, const Slot<double>& sd, double p, double dx,
+                                double invdx, CellCounters& cc) {
     const int n = M.n;
     double *y0 = s.v(0), *yTemp = s.v(1), *k1 = s.v(2), *k2 = s.v(3), *k3 = s.v(4), *k4 = s.v(5);
     double *err = s.v(8), *dydx = s.v(9), *dfdx = s.v(10), *tmp = s.v(11);
@@ -186,16 +295,15 @@ __device__ __noinline__ double ros34_attempt(const Grp<G>& g, const DevMech& M, 
     const double d1 = 1.0 / 2.0, d2 = -3.0 / 2.0, d3 = 605.0 / 250.0, d4 = 29.0 / 250.0;
     const double invgamma = 1.0 / (1.0 / 2.0);
 
-    jac_eval<G, MT>(g, M, s, p, y0, dfdx, s.J, o.jacobian);
+    jacobian_into<G, MT>(g, M, s, sd, p, y0, dfdx, o.jacobian);
     const double cdiag = invdx * invgamma;
-    form_iteration_matrix<G, MT>(g, s, n, cdiag);
-    lu_factor<G, MT>(g, s.LU, n, s.ld, s.piv, s.invD);
+    factor_iteration<G, MT>(g, M, s, cdiag);
     cc.jac++; cc.lu++; cc.rhs += 2; cc.solves += 4;
 
     const double dxd1 = dx * d1 + 1;
     for (int i = g.rank; i < n; i += G) k1[i] = dxd1 * dfdx[i];
     g.sync();
-    linear_solve<G, MT>(g, M, s, cdiag, k1, tmp);
+    if (!stage_solve<G, MT>(g, M, s, cdiag, k1, tmp)) return -1.0;
     for (int i = g.rank; i < n; i += G) yTemp[i] = fma(a21, k1[i], y0[i]);
     g.sync();
     rhs_eval<G, MT>(g, M, s, p, yTemp, dydx, 1);
@@ -204,7 +312,7 @@ __device__ __noinline__ double ros34_attempt(const Grp<G>& g, const DevMech& M, 
         for (int i = g.rank; i < n; i += G) k2[i] = fma(f1, k1[i], fma(dxd2, dfdx[i], dydx[i]));
     }
     g.sync();
-    linear_solve<G, MT>(g, M, s, cdiag, k2, tmp);
+    if (!stage_solve<G, MT>(g, M, s, cdiag, k2, tmp)) return -1.0;
     for (int i = g.rank; i < n; i += G) yTemp[i] = fma(a32, k2[i], fma(a31, k1[i], y0[i]));
     g.sync();
     rhs_eval<G, MT>(g, M, s, p, yTemp, dydx, 1);
@@ -213,14 +321,14 @@ __device__ __noinline__ double ros34_attempt(const Grp<G>& g, const DevMech& M, 
         for (int i = g.rank; i < n; i += G) k3[i] = fma(f2, k2[i], fma(f1, k1[i], fma(dxd3, dfdx[i], dydx[i])));
     }
     g.sync();
-    linear_solve<G, MT>(g, M, s, cdiag, k3, tmp);
+    if (!stage_solve<G, MT>(g, M, s, cdiag, k3, tmp)) return -1.0;
     {
         const double dxd4 = dx * d4, f1 = c41 * invdx, f2 = c42 * invdx, f3 = c43 * invdx;
         for (int i = g.rank; i < n; i += G)
             k4[i] = fma(f3, k3[i], fma(f2, k2[i], fma(f1, k1[i], fma(dxd4, dfdx[i], dydx[i]))));
     }
     g.sync();
-    linear_solve<G, MT>(g, M, s, cdiag, k4, tmp);
+    if (!stage_solve<G, MT>(g, M, s, cdiag, k4, tmp)) return -1.0;
     double me = 0;
     for (int i = g.rank; i < n; i += G) {
         const double yt = fma(b4, k4[i], fma(b3, k3[i], fma(b2, k2[i], fma(b1, k1[i], y0[i]))));
@@ -236,10 +344,28 @@ __device__ __noinline__ double ros34_attempt(const Grp<G>& g, const DevMech& M, 
 
 // ODESolve + adaptiveSolve (OptRodas34.C:123-289, OptRosenbrock34.C:127-279),
 // with bounded reject loops.  Returns FCS_CELL_*; y0 (vector 0) holds the state.
+// One attempt in the slot's precision; in mixed precision an attempt whose
+// FP32 factorisation fails the refinement check is redone in FP64.
+template<int G, class MT>
+__device__ __forceinline__ double rosenbrock_attempt(const Grp<G>& g, const DevMech& M, const KOpts& o,
+                                                     const Slot<MT>& s, const Slot<double>& sd, double p,
+                                                     double dx, double invdx, CellCounters& cc) {
+    double Err = o.solver == FCS_SOLVER_RODAS34 ? rodas34_attempt<G, MT>(g, M, o, s, sd, p, dx, invdx, cc)
+                                                : ros34_attempt<G, MT>(g, M, o, s, sd, p, dx, invdx, cc);
+    if constexpr (sizeof(MT) == 4) {
+        if (Err == -1.0) {
+            cc.fallbacks++;
+            Err = o.solver == FCS_SOLVER_RODAS34 ? rodas34_attempt<G, double>(g, M, o, sd, sd, p, dx, invdx, cc)
+                                                 : ros34_attempt<G, double>(g, M, o, sd, sd, p, dx, invdx, cc);
+        }
+    }
+    return Err;
+}
+
 template<int G, class MT>
 __device__ int rosenbrock_integrate(const Grp<G>& g, const DevMech& M, const KOpts& o,
-                                    const Slot<MT>& s, double p, double xEnd, double& dxTryIO,
-                                    CellCounters& cc) {
+                                    const Slot<MT>& s, const Slot<double>& sd, double p, double xEnd,
+                                    double& dxTryIO, CellCounters& cc) {
     const double SAFE = 0.9, ALPHA_INC = 0.2, ALPHA_DEC = 0.25, MIN_SCALE = 0.2, MAX_SCALE = 10;
     const double ratio = 5.904900000000001e-06;  // (MAX_SCALE/SAFE)^(-1/ALPHA_INC)
     const double safeMaxScale = SAFE * MAX_SCALE;
@@ -253,9 +379,7 @@ __device__ int rosenbrock_integrate(const Grp<G>& g, const DevMech& M, const KOp
         const double dxTry0 = dxTry;
         if ((x + dxTry - xEnd) * (x + dxTry - 0.0) > 0) { last = true; dxTry = xEnd - x; }
         double dx = dxTry, invdx = 1.0 / dx;
-        double Err = o.solver == FCS_SOLVER_RODAS34
-                         ? rodas34_attempt<G, MT>(g, M, o, s, p, dx, invdx, cc)
-                         : ros34_attempt<G, MT>(g, M, o, s, p, dx, invdx, cc);
+        double Err = rosenbrock_attempt<G, MT>(g, M, o, s, sd, p, dx, invdx, cc);
         cc.attempts++;
         int rejects = 0;
         while (Err > 1) {
@@ -263,9 +387,7 @@ __device__ int rosenbrock_integrate(const Grp<G>& g, const DevMech& M, const KOp
             const double scale = fmax(SAFE * pow(Err, -ALPHA_DEC), MIN_SCALE);
             dx *= scale;
             invdx = 1.0 / dx;
-            Err = o.solver == FCS_SOLVER_RODAS34
-                      ? rodas34_attempt<G, MT>(g, M, o, s, p, dx, invdx, cc)
-                      : ros34_attempt<G, MT>(g, M, o, s, p, dx, invdx, cc);
+            Err = rosenbrock_attempt<G, MT>(g, M, o, s, sd, p, dx, invdx, cc);
             cc.attempts++;
         }
         if (!(Err == Err)) return FCS_CELL_NONFINITE;
@@ -318,20 +440,21 @@ struct SeulexState {
     double dxOpt[kIMax], temp[kIMax];
 };
 
+// returns 1 on success, 0 when the sequence diverged (step reject), 2 when the
+// mixed-precision solve needs FP64
 template<int G, class MT>
-__device__ __noinline__ bool seul(const Grp<G>& g, const DevMech& M, const Slot<MT>& s, double p,
+__device__ __noinline__ int seul(const Grp<G>& g, const DevMech& M, const Slot<MT>& s, double p,
                      const SeulexConst& sc, SeulexState& st, double dxTot, int k, CellCounters& cc) {
     const int n = M.n;
     double *y0_ = s.v(1), *ySeq = s.v(2), *scale = s.v(3), *yTemp = s.v(4), *dy = s.v(5), *dydx = s.v(6);
     double* tmp = s.v(11);
     const int nSteps = sc.nSeq[k];
     const double invdx = nSteps / dxTot;
-    form_iteration_matrix<G, MT>(g, s, n, invdx);
-    lu_factor<G, MT>(g, s.LU, n, s.ld, s.piv, s.invD);
+    factor_iteration<G, MT>(g, M, s, invdx);
     cc.lu++;
     rhs_eval<G, MT>(g, M, s, p, y0_, dy, 1);
     cc.rhs++;
-    linear_solve<G, MT>(g, M, s, invdx, dy, tmp);
+    if (!stage_solve<G, MT>(g, M, s, invdx, dy, tmp)) return 2;
     cc.solves++;
     for (int i = g.rank; i < n; i += G) yTemp[i] = y0_[i];
     g.sync();
@@ -347,7 +470,7 @@ __device__ __noinline__ bool seul(const Grp<G>& g, const DevMech& M, const Slot<
             cc.rhs++;
             for (int i = g.rank; i < n; i += G) dy[i] = dydx[i] - dy[i] * invdx;
             g.sync();
-            linear_solve<G, MT>(g, M, s, invdx, dy, tmp);
+            if (!stage_solve<G, MT>(g, M, s, invdx, dy, tmp)) return 2;
             cc.solves++;
             // dy2 = vGreat as soon as one |dy_i| > sqrt(vGreat)
             double b = 0, big = 0;
@@ -359,24 +482,24 @@ __device__ __noinline__ bool seul(const Grp<G>& g, const DevMech& M, const Slot<
             gsum2(g, b, big, s.red);
             const double dy2 = big > 0 ? 1e300 : sqrt(b);
             st.theta = dy2 / fmax(1.0, dy1 + kSmall);
-            if (st.theta > 1.0) return false;
+            if (st.theta > 1.0) return 0;
         }
         rhs_eval<G, MT>(g, M, s, p, yTemp, dy, 1);
         cc.rhs++;
-        linear_solve<G, MT>(g, M, s, invdx, dy, tmp);
+        if (!stage_solve<G, MT>(g, M, s, invdx, dy, tmp)) return 2;
         cc.solves++;
     }
     for (int i = g.rank; i < n; i += G) ySeq[i] = yTemp[i] + dy[i];
     g.sync();
-    return true;
+    return 1;
 }
 
-struct SeulexStep { double dxTry; bool first, last, reject, prevReject, failed; };
+struct SeulexStep { double dxTry; bool first, last, reject, prevReject, failed, needFp64; };
 
 template<int G, class MT>
 __device__ __noinline__ void seulex_step(const Grp<G>& g, const DevMech& M, const KOpts& o, const Slot<MT>& s,
-                            double p, const SeulexConst& sc, SeulexState& st, double& x,
-                            SeulexStep& step, CellCounters& cc) {
+                            const Slot<double>& sd, double p, const SeulexConst& sc, SeulexState& st,
+                            double& x, SeulexStep& step, CellCounters& cc) {
     const int n = M.n;
     double *y = s.v(0), *y0_ = s.v(1), *ySeq = s.v(2), *scale = s.v(3), *k9 = s.v(7);
     double* table = s.table;
@@ -398,7 +521,7 @@ __device__ __noinline__ void seulex_step(const Grp<G>& g, const DevMech& M, cons
     }
     bool jacUpdated = false;
     if (st.theta > jacRedo) {
-        jac_eval<G, MT>(g, M, s, p, y, k9, s.J, o.jacobian);
+        jacobian_into<G, MT>(g, M, s, sd, p, y, k9, o.jacobian);
         cc.jac++;
         jacUpdated = true;
     }
@@ -414,8 +537,9 @@ __device__ __noinline__ void seulex_step(const Grp<G>& g, const DevMech& M, cons
         double errOld = 0;
         cc.attempts++;
         for (k = 0; k <= st.kTarg + 1; k++) {
-            const bool ok = seul<G, MT>(g, M, s, p, sc, st, dx, k, cc);
-            if (!ok) { step.reject = true; dxNew = fabs(dx) * 0.5; break; }
+            const int ok = seul<G, MT>(g, M, s, p, sc, st, dx, k, cc);
+            if (ok == 2) { step.needFp64 = true; return; }
+            if (ok == 0) { step.reject = true; dxNew = fabs(dx) * 0.5; break; }
             if (k == 0) {
                 for (int i = g.rank; i < n; i += G) y[i] = ySeq[i];
             } else {
@@ -491,7 +615,7 @@ __device__ __noinline__ void seulex_step(const Grp<G>& g, const DevMech& M, cons
             step.prevReject = true;
             if (!jacUpdated) {
                 st.theta = 2.0 * jacRedo;
-                jac_eval<G, MT>(g, M, s, p, y, k9, s.J, o.jacobian);
+                jacobian_into<G, MT>(g, M, s, sd, p, y, k9, o.jacobian);
                 cc.jac++;
                 jacUpdated = true;
             }
@@ -524,21 +648,26 @@ __device__ __noinline__ void seulex_step(const Grp<G>& g, const DevMech& M, cons
     step.dxTry = dxNew;
 }
 
+// Internal status: the mixed-precision integration of this cell must be redone in FP64.
+constexpr int kNeedFp64 = 100;
+
 template<int G, class MT>
 __device__ int seulex_integrate(const Grp<G>& g, const DevMech& M, const KOpts& o, const Slot<MT>& s,
-                                double p, double xEnd, double& dxTryIO, CellCounters& cc) {
+                                const Slot<double>& sd, double p, double xEnd, double& dxTryIO,
+                                CellCounters& cc) {
     const SeulexConst sc = seulex_const();
     SeulexState st;
     st.theta = 0; st.kTarg = 1;
     for (int i = 0; i < kIMax; i++) { st.dxOpt[i] = 0; st.temp[i] = 0; }
-    SeulexStep step{dxTryIO, true, false, false, false, false};
+    SeulexStep step{dxTryIO, true, false, false, false, false, false};
     double x = 0;
     const int n = M.n;
     for (int nStep = 0; nStep < o.maxSteps; nStep++) {
         const double dxTry0 = step.dxTry;
         step.reject = false;
         if ((x + step.dxTry - xEnd) * (x + step.dxTry - 0.0) > 0) { step.last = true; step.dxTry = xEnd - x; }
-        seulex_step<G, MT>(g, M, o, s, p, sc, st, x, step, cc);
+        seulex_step<G, MT>(g, M, o, s, sd, p, sc, st, x, step, cc);
+        if (step.needFp64) return kNeedFp64;
         if (step.failed) return FCS_CELL_DT_UNDERFLOW;
         cc.accepted++;
         double bad = 0;
@@ -575,6 +704,7 @@ integrate_kernel(const DevMech M, const KOpts o, const SlotLayout L, CellIO io, 
     if (gws) base = gws + (size_t)(blockIdx.x * groupsPerBlock + gidInBlock) * L.bytes;
     else base = smem + (size_t)gidInBlock * L.bytes;
     const Slot<MT> s = make_slot<MT>(base, L, M);
+    const Slot<double> sd = make_slot<double>(base, L, M);
     const int ns = M.ns, n = M.n;
     CellCounters cc;
     long long nCells = 0, nFailed = 0;
@@ -598,13 +728,31 @@ integrate_kernel(const DevMech M, const KOpts o, const SlotLayout L, CellIO io, 
         }
         if (g.rank == 0) y[ns] = T0;
         g.sync();
-        double subDt = io.subDt[c];
+        const double subDt0 = io.subDt[c];
+        double subDt = subDt0;
         int st = FCS_CELL_OK;
         double timeLeft = deltaT;
         while (timeLeft > kSmall) {
             const double dtc = timeLeft;
-            if (o.solver == FCS_SOLVER_SEULEX) st = seulex_integrate<G, MT>(g, M, o, s, p, dtc, subDt, cc);
-            else st = rosenbrock_integrate<G, MT>(g, M, o, s, p, dtc, subDt, cc);
+            if (o.solver == FCS_SOLVER_SEULEX) {
+                st = seulex_integrate<G, MT>(g, M, o, s, sd, p, dtc, subDt, cc);
+                if constexpr (sizeof(MT) == 4) {
+                    if (st == kNeedFp64) {
+                        // redo the whole cell in FP64 from its initial state
+                        cc.fallbacks++;
+                        for (int i = g.rank; i < ns; i += G) {
+                            const double Yi = io.Y[(size_t)i * nc + c];
+                            y[i] = Yi > 0 ? Yi : 0.0;
+                        }
+                        if (g.rank == 0) y[ns] = T0;
+                        g.sync();
+                        subDt = subDt0;
+                        st = seulex_integrate<G, double>(g, M, o, sd, sd, p, dtc, subDt, cc);
+                    }
+                }
+            } else {
+                st = rosenbrock_integrate<G, MT>(g, M, o, s, sd, p, dtc, subDt, cc);
+            }
             timeLeft -= dtc;
             if (st != FCS_CELL_OK) break;
         }
@@ -635,6 +783,7 @@ integrate_kernel(const DevMech M, const KOpts o, const SlotLayout L, CellIO io, 
         atomicAdd(reinterpret_cast<unsigned long long*>(&io.stats[ST_LU]), (unsigned long long)cc.lu);
         atomicAdd(reinterpret_cast<unsigned long long*>(&io.stats[ST_RHS]), (unsigned long long)cc.rhs);
         atomicAdd(reinterpret_cast<unsigned long long*>(&io.stats[ST_SOLVES]), (unsigned long long)cc.solves);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&io.stats[ST_FALLBACK]), (unsigned long long)cc.fallbacks);
         if (nCells) atomicMin(io.dtMinBits, dbits(dtMin));
     }
 }
@@ -665,10 +814,11 @@ eval_kernel(const DevMech M, const KOpts o, const SlotLayout L, long long nc, co
     if (mode == 0) {
         rhs_eval<G, MT>(g, M, s, p[c], y, f, 1);
     } else if (mode == 1) {
-        jac_eval<G, MT>(g, M, s, p[c], y, f, s.J, o.jacobian);
+        const Slot<double> sd = make_slot<double>(base, L, M);
+        jac_eval<G, double>(g, M, sd, p[c], y, f, sd.J, o.jacobian);
         for (int idx = g.rank; idx < n * n; idx += G) {
             const int i = idx / n, j = idx - i * n;
-            Jout[(size_t)c * n * n + idx] = double(s.J[(size_t)i * s.ld + j]);
+            Jout[(size_t)c * n * n + idx] = sd.J[(size_t)i * s.ld + j];
         }
     } else {
         const double qd = rates_eval<G, MT>(g, M, s, p[c], T[c], rho[c], y, f);

@@ -28,7 +28,7 @@ ERRORS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "STATE", 5: "CELLS", 
 EXPORTS = ("fcs_create", "fcs_destroy", "fcs_last_error_string", "fcs_version", "fcs_load_mechanism",
            "fcs_load_mechanism_foam", "fcs_read_chemistry_properties", "fcs_default_options",
            "fcs_set_options", "fcs_mechanism_size", "fcs_integrate", "fcs_integrate_lts", "fcs_rhs",
-           "fcs_jacobian", "fcs_rates")
+           "fcs_jacobian", "fcs_rates", "fcs_bench_fp64_peak", "fcs_bench_fp32_peak", "fcs_check_exp")
 
 
 class MechDesc(C.Structure):
@@ -54,7 +54,7 @@ class StepStats(C.Structure):
                 ("cells_failed", C.c_int64), ("attempts", C.c_int64), ("accepted", C.c_int64),
                 ("jacobians", C.c_int64), ("lu_decompositions", C.c_int64),
                 ("rhs_evaluations", C.c_int64), ("linear_solves", C.c_int64),
-                ("kernel_ms", C.c_double)]
+                ("fp64_fallbacks", C.c_int64), ("kernel_ms", C.c_double), ("call_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -89,6 +89,9 @@ def load(path: str = LIB) -> C.CDLL:
     L.fcs_rhs.argtypes = [vp, C.c_int64, vp, vp, vp, vp, C.c_int32]
     L.fcs_jacobian.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, C.c_int32]
     L.fcs_rates.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, vp, C.c_int32]
+    L.fcs_bench_fp64_peak.argtypes = [C.c_int, C.c_double, _dp]
+    L.fcs_bench_fp32_peak.argtypes = [C.c_int, C.c_double, _dp]
+    L.fcs_check_exp.argtypes = [C.c_int, C.c_longlong, vp, vp, vp]
     _LIB = L
     return L
 
@@ -130,6 +133,37 @@ def make_desc(flat) -> MechDesc:
     d.plog_offset = p(flat.plog_offset, C.c_int32); d.plog_table = p(flat.plog_table, C.c_double)
     d._keep = keep
     return d
+
+
+def fp64_peak_tflops(device: int = 0, ms: float = 50.0) -> float:
+    """Measured dense FP64 FMA throughput of the device (TFLOP/s)."""
+    L = load()
+    v = C.c_double(0)
+    st = L.fcs_bench_fp64_peak(device, ms, C.byref(v))
+    if st:
+        raise FcsError(st, "fp64 peak probe failed")
+    return v.value
+
+
+def fp32_peak_tflops(device: int = 0, ms: float = 50.0) -> float:
+    L = load()
+    v = C.c_double(0)
+    st = L.fcs_bench_fp32_peak(device, ms, C.byref(v))
+    if st:
+        raise FcsError(st, "fp32 peak probe failed")
+    return v.value
+
+
+def check_exp(x, device: int = 0):
+    """(integrator exp, CUDA exp) of the host array x."""
+    L = load()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    a = np.empty_like(x)
+    b = np.empty_like(x)
+    st = L.fcs_check_exp(device, x.size, x.ctypes.data, a.ctypes.data, b.ctypes.data)
+    if st:
+        raise FcsError(st, "exp check failed")
+    return a, b
 
 
 def read_chemistry_properties(path: str):
@@ -204,7 +238,7 @@ class Context:
                                           _addr(Y), _addr(sub), _addr(RR), _addr(status), C.byref(stats),
                                           C.byref(dmin), flags)
         else:
-            st = self.L.fcs_integrate(self.h, n, dt, _addr(p), _addr(rho0), _addr(T), _addr(Y), _addr(sub),
+            st = self.L.fcs_integrate(self.h, n, 0.0 if dt is None else dt, _addr(p), _addr(rho0), _addr(T), _addr(Y), _addr(sub),
                                       _addr(RR), _addr(status), C.byref(stats), C.byref(dmin), flags)
         if check and st not in (0, 5):
             self._check(st)

@@ -136,7 +136,7 @@ typedef struct fcs_options {
     double abs_tol;
     double rel_tol;
     int32_t max_steps;           /* default 10000                     */
-    int32_t max_rejects;         /* bound on rejected retries per step (GPU-only, default 64) */
+    int32_t max_rejects;         /* bound on rejected retries per step (GPU-only, default 1000) */
     double T_react;              /* cells with T <= Treact are skipped */
     double delta_t_chem_max;     /* maxChemicalTimeStep (default 1e300) */
 } fcs_options;
@@ -152,7 +152,11 @@ typedef struct fcs_step_stats {
     int64_t lu_decompositions;
     int64_t rhs_evaluations;
     int64_t linear_solves;
+    int64_t fp64_fallbacks;      /* mixed precision: attempts (Rosenbrock) or cells (Seulex)
+                                    redone in FP64 after a failed refinement check */
     double  kernel_ms;           /* device time of the integration kernel */
+    double  call_ms;             /* device time of the whole call on the library's
+                                    stream, host<->device copies included */
 } fcs_step_stats;
 
 fcs_status fcs_create(fcs_ctx** ctx, int device);

@@ -1277,3 +1277,31 @@ int32_t orc_jacobian(const orc_mech* m, const orc_options* o, int64_t n_cells,
     ws_destroy(w);
     return FCS_OK;
 }
+
+/* FastChemistryModel::calculate (FastChemistryModel.C:715-755): c_i = rho Y_i / W_i
+ * (no clamp), RR_i = dNdtByV_i W_i; Qdot = -sum Hf_i RR_i (FastChemistryModel.C:656-685)
+ * with Hf the janaf enthalpy at 298.15 K. */
+int32_t orc_rates(const orc_mech* m, int64_t n_cells, const double* p, const double* T, const double* rho,
+                  const double* Y, double* RR, double* Qdot)
+{
+    ws_t* w = ws_create(m);
+    const int ns = m->ns;
+    double* om = (double*)malloc(sizeof(double) * ns);
+    for (int64_t c = 0; c < n_cells; c++) {
+        for (int i = 0; i < ns; i++) w->C[i] = rho[c] * Y[(size_t)i * n_cells + c] / m->W[i];
+        dNdtByV(m, w, p[c], T[c], om, w->Cp, w->Ha, T[c], 1);
+        double q = 0;
+        for (int i = 0; i < ns; i++) {
+            const double rr = om[i] * m->W[i];
+            RR[(size_t)i * n_cells + c] = rr;
+            const double* a = (298.15 < m->Tcommon[i]) ? &m->coef[i * 14] : &m->coef[i * 14 + 7];
+            const double t = 298.15;
+            const double hf = RU * m->invW[i] * (((((a[4] / 5 * t + a[3] / 4) * t + a[2] / 3) * t + a[1] / 2) * t + a[0]) * t + a[5]);
+            q -= hf * rr;
+        }
+        if (Qdot) Qdot[c] = q;
+    }
+    free(om);
+    ws_destroy(w);
+    return FCS_OK;
+}

@@ -102,6 +102,7 @@ class Port:
         L.orc_jacobian.argtypes = [C.c_void_p, C.POINTER(OrcOptions), C.c_int64, _dp, _dp, _dp, _dp, _dp]
         L.orc_lu_solve.argtypes = [C.c_int32, _dp, C.c_int32, _dp, _ip, _dp]
         L.orc_mech_order.argtypes = [C.c_void_p, _ip]
+        L.orc_rates.argtypes = [C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp]
         self.ns = flat.n_species
         self.nr = flat.n_reactions
         self.desc = make_desc(flat)
@@ -171,6 +172,14 @@ class Port:
                               _ptr(np.ascontiguousarray(T)), _ptr(np.ascontiguousarray(Y)),
                               _ptr(J), _ptr(f))
         return J, f
+
+    def rates(self, p, T, rho, Y):
+        n = T.shape[0]
+        RR = np.zeros((self.ns, n))
+        Q = np.zeros(n)
+        self.lib.orc_rates(self.h, n, _ptr(np.ascontiguousarray(p)), _ptr(np.ascontiguousarray(T)),
+                           _ptr(np.ascontiguousarray(rho)), _ptr(np.ascontiguousarray(Y)), _ptr(RR), _ptr(Q))
+        return RR, Q
 
     def lu_solve(self, a, b):
         a = np.ascontiguousarray(a, dtype=np.float64).copy()
