@@ -269,13 +269,14 @@ def main():
     hRR = torch.zeros_like(hY).pin_memory()
     hst = torch.zeros(n, dtype=torch.int32).pin_memory()
     e2e_ms = []
-    for i in range(args.warmup + args.steps):
+    e2e_warm = 1  # the device path above is already warm
+    for i in range(e2e_warm + args.steps):
         hT.copy_(hp["T"]); hY.copy_(hp["Y"]); hS.copy_(hp["subDt"])
         flush.zero_()
         torch.cuda.synchronize()
         code, stats, dmin = ctx.integrate_raw(n, w.dt, hp["p"].numpy(), hp["rho0"].numpy(), hT.numpy(), hY.numpy(),
                                               hS.numpy(), hRR.numpy(), hst.numpy())
-        if i >= args.warmup:
+        if i >= e2e_warm:
             e2e_ms.append(stats["call_ms"])
     t_e2e = statistics.mean(e2e_ms)
     if ws > 1:

@@ -383,9 +383,62 @@ static fcs_status ensure_gws(fcs_ctx* ctx, const Shape& sh) {
 
 static int default_group(fcs_ctx* ctx) {
     const int n = ctx->M.n;
-    if (n <= 64) return 32;
     if (n <= 128) return 64;
     return 128;
+}
+
+// Autotuner for FCS_MAPPING_AUTO: times every candidate cell-to-thread
+// mapping on the first `sample` queued cells, integrated from copies of their
+// state (the caller's arrays are not touched), and keeps the fastest for this
+// (mechanism size, precision, solver, Jacobian) key.
+static int tuned_group(fcs_ctx* ctx, const CellIO& io, int nActive) {
+    const auto key = std::make_tuple(ctx->M.n, (int)ctx->opt.precision, (int)ctx->opt.solver, (int)ctx->opt.jacobian);
+    auto it = ctx->tuned.find(key);
+    if (it != ctx->tuned.end()) return it->second;
+    const int fallback = default_group(ctx);
+    if (nActive < 2048) return fallback;  // too few cells to time reliably; not cached
+    const int ns = ctx->M.ns;
+    const long long nc = io.nCells;
+    cudaStream_t st = ctx->stream;
+    DBuf<double> T, Y, S;
+    DBuf<int> stat, head;
+    if (T.ensure(nc) || Y.ensure((size_t)ns * nc) || S.ensure(nc) || stat.ensure(nc) || head.ensure(1)) {
+        T.release(); Y.release(); S.release(); stat.release(); head.release();
+        return fallback;
+    }
+    const KOpts ko = kopts(ctx->opt);
+    int best = fallback;
+    float bestMs = 1e30f;
+    for (int g : {32, 64, 128, 256}) {
+        Shape sh;
+        if (!make_shape(ctx, g, true, sh)) continue;
+        if (ensure_gws(ctx, sh) != FCS_OK) continue;
+        const int groups = sh.lc.grid * (sh.lc.block / g);
+        const int sample = std::min(nActive, 2 * groups);
+        CellIO sio = io;
+        sio.T = T.p; sio.Y = Y.p; sio.subDt = S.p; sio.RR = nullptr; sio.status = stat.p;
+        cudaMemcpyAsync(T.p, io.T, nc * 8, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(Y.p, io.Y, (size_t)ns * nc * 8, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(S.p, io.subDt, nc * 8, cudaMemcpyDeviceToDevice, st);
+        cudaMemsetAsync(head.p, 0, sizeof(int), st);
+        WorkQueue q{head.p, ctx->bOrder.p, sample};
+        cudaEventRecord(ctx->ev0, st);
+        const cudaError_t e = launch_integrate(sh.lc, sh.mixed, ctx->M, ko, sh.L, sio, q,
+                                               sh.global ? ctx->gws.p : nullptr, st);
+        cudaEventRecord(ctx->ev1, st);
+        if (e != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) continue;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        const float perCell = ms / sample;
+        if (perCell < bestMs) { bestMs = perCell; best = g; }
+    }
+    T.release(); Y.release(); S.release(); stat.release(); head.release();
+    // the statistics of the sample runs are not the caller's
+    cudaMemsetAsync(ctx->bStats.p, 0, ST_COUNT * sizeof(long long), st);
+    cudaMemsetAsync(ctx->bMin.p, 0x7f, sizeof(unsigned long long), st);
+    cudaStreamSynchronize(st);
+    ctx->tuned[key] = best;
+    return best;
 }
 
 // ------------------------------------------------------------------------
@@ -440,7 +493,7 @@ static fcs_status integrate_impl(fcs_ctx* ctx, int64_t nc, double dt, const doub
     int nActive = 0;
     CK(cudaMemcpyAsync(&nActive, ctx->bHead.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    const int group = ctx->opt.mapping ? ctx->opt.mapping : default_group(ctx);
+    const int group = ctx->opt.mapping ? ctx->opt.mapping : tuned_group(ctx, io, nActive);
     Shape sh;
     if (!make_shape(ctx, group, true, sh))
         return set_err(ctx, FCS_ERR_UNSUPPORTED, "no launch shape for this mapping");
@@ -480,6 +533,8 @@ static fcs_status integrate_impl(fcs_ctx* ctx, int64_t nc, double dt, const doub
         stats->fp64_fallbacks = hs[ST_FALLBACK];
         stats->kernel_ms = ms;
         stats->call_ms = cms;
+        stats->mapping = group;
+        stats->reserved = 0;
     }
     if (dtMin) {
         double m = 1e15;  // great

@@ -95,6 +95,7 @@ struct SlotLayout {
     int offJ64, offLU64;  // FP64 views of the Jacobian / LU factors (LU64 == J64: in place)
     int offJ32, offLU32;  // FP32 views (mixed precision), inside the same matrix region
     int offVec;        // kNV vectors of n doubles
+    int offVec32;      // 2 vectors of n floats (mixed-precision solves)
     int offSp;         // 7 species arrays (C, E, Einv, Cp, Ha, dBdT, dCpdT) [ns]
     int offInvD;       // [n] double
     int offScale;      // row / column equilibration factors [2n] double (mixed precision)
@@ -106,7 +107,7 @@ struct SlotLayout {
     int bytes;         // total, multiple of 16
 };
 
-constexpr int kNV = 16;  // stage / work vectors per slot
+constexpr int kNV = 12;  // stage / work vectors per slot
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 
@@ -123,12 +124,13 @@ __host__ __device__ inline SlotLayout make_layout(int ns, int nr, int nTB, bool 
     const int m64 = align16(n * L.ld * 8), m32 = align16(n * L.ld * 4);
     int o = 0;
     L.offJ64 = 0;
-    if (seulex) { L.offLU64 = m64; o = 2 * m64; }
-    else if (mixed) { L.offLU64 = 0; o = 2 * m32 > m64 ? 2 * m32 : m64; }
-    else { L.offLU64 = 0; o = m64; }
-    L.offJ32 = 0;
-    L.offLU32 = m32;
+    if (seulex) { L.offLU64 = m64; o = 2 * m64; }   // FP64 Jacobian (kept) + FP64 LU
+    else if (mixed) { L.offLU64 = 0; o = m64 + m32; } // FP64 Jacobian (kept) + FP32 LU; FP64 fallback in place
+    else { L.offLU64 = 0; o = m64; }                 // FP64 matrix factored in place
+    L.offJ32 = 0;                                    // (unused: the Jacobian stays FP64)
+    L.offLU32 = m64;                                 // after the FP64 Jacobian (inside LU64 for Seulex)
     L.offVec = o;   o = align16(o + kNV * n * 8);
+    L.offVec32 = o; o = align16(o + 2 * n * 4);
     L.offSp = o;    o = align16(o + 7 * ns * 8);
     L.offInvD = o;  o = align16(o + n * 8);
     L.offScale = o; o = align16(o + 2 * n * 8);
@@ -148,6 +150,8 @@ struct Slot {
     MT* J;
     MT* LU;
     double* vec;      // vec + k*n is vector k
+    float *x32, *r32; // FP32 solve vectors (mixed precision)
+    double* J64;      // the FP64 Jacobian (== J for MT = double)
     double *C, *B, *Binv, *Cp, *Ha, *dBdT, *dCpdT;   // B = exp(-G/RT), Binv = 1/B
     double* invD;
     double *dr, *dc;
@@ -171,6 +175,9 @@ __device__ __forceinline__ Slot<MT> make_slot(char* base, const SlotLayout& L, c
         s.LU = reinterpret_cast<MT*>(base + L.offLU32);
     }
     s.vec = reinterpret_cast<double*>(base + L.offVec);
+    s.x32 = reinterpret_cast<float*>(base + L.offVec32);
+    s.r32 = s.x32 + M.n;
+    s.J64 = reinterpret_cast<double*>(base + L.offJ64);
     double* sp = reinterpret_cast<double*>(base + L.offSp);
     s.C = sp; s.B = sp + M.ns; s.Binv = sp + 2 * M.ns; s.Cp = sp + 3 * M.ns; s.Ha = sp + 4 * M.ns;
     s.dBdT = sp + 5 * M.ns; s.dCpdT = sp + 6 * M.ns;
@@ -809,17 +816,17 @@ __device__ __noinline__ void lu_factor(const Grp<G>& g, MT* A, int n, int ld, in
 // does the column sweeps (shared-memory vector, one __syncwarp per column);
 // the other warps wait at the closing group barrier.  b is a slot vector of
 // doubles; arithmetic in MT.
-template<int G, class MT>
+template<int G, class MT, class VT>
 __device__ __noinline__ void lu_solve(const Grp<G>& g, const MT* A, int n, int ld, const int* perm,
-                                      const double* invD, double* b) {
+                                      const double* invD, VT* b) {
     g.sync();
     if (g.rank < 32) {
         const int lane = g.rank;
-        double t[8];
+        VT t[8];
 #pragma unroll
         for (int u = 0; u < 8; u++) {
             const int i = lane + 32 * u;
-            t[u] = i < n ? b[perm[i]] : 0.0;
+            t[u] = i < n ? b[perm[i]] : VT(0);
         }
         __syncwarp();
 #pragma unroll
@@ -829,15 +836,15 @@ __device__ __noinline__ void lu_solve(const Grp<G>& g, const MT* A, int n, int l
         }
         __syncwarp();
         for (int j = 0; j < n - 1; j++) {
-            const MT bj = MT(b[j]);
-            for (int i = j + 1 + lane; i < n; i += 32) b[i] = double(fma(-A[(size_t)i * ld + j], bj, MT(b[i])));
+            const VT bj = b[j];
+            for (int i = j + 1 + lane; i < n; i += 32) b[i] = fma(-VT(A[(size_t)i * ld + j]), bj, b[i]);
             __syncwarp();
         }
         for (int j = n - 1; j >= 0; j--) {
-            const MT xj = MT(b[j]) * MT(invD[j]);
-            for (int i = lane; i < j; i += 32) b[i] = double(fma(-A[(size_t)i * ld + j], xj, MT(b[i])));
+            const VT xj = b[j] * VT(invD[j]);
+            for (int i = lane; i < j; i += 32) b[i] = fma(-VT(A[(size_t)i * ld + j]), xj, b[i]);
             __syncwarp();
-            if (lane == (j & 31)) b[j] = double(xj);
+            if (lane == (j & 31)) b[j] = xj;
         }
         __syncwarp();
     }

@@ -34,30 +34,6 @@ struct CellCounters {
 // and the attempt is redone in FP64.
 constexpr double kRefineTol = 1e-3;
 
-// FP64 Jacobian (assembled in the FP64 view of the matrix region) -> FP32
-// Jacobian at the start of the same region.  Rounds of G*R elements: every
-// element a round overwrites (bytes [4k, 4k+4)) was read in this or an
-// earlier round, so the in-place narrowing is race free.
-template<int G>
-__device__ __noinline__ void jac_to_fp32(const Grp<G>& g, const double* J64, float* J32, int count) {
-    constexpr int R = 4;
-    for (int start = 0; start < count; start += G * R) {
-        double v[R];
-#pragma unroll
-        for (int r = 0; r < R; r++) {
-            const int k = start + r * G + g.rank;
-            v[r] = k < count ? J64[k] : 0.0;
-        }
-        g.sync();
-#pragma unroll
-        for (int r = 0; r < R; r++) {
-            const int k = start + r * G + g.rank;
-            if (k < count) J32[k] = float(v[r]);
-        }
-        g.sync();
-    }
-}
-
 // FP64: A = c I - J into the LU view (in place for the single-matrix layout)
 template<int G>
 __device__ __noinline__ void form_iteration_matrix(const Grp<G>& g, const Slot<double>& s, int n, double c) {
@@ -71,75 +47,71 @@ __device__ __noinline__ void form_iteration_matrix(const Grp<G>& g, const Slot<d
     g.sync();
 }
 
-__device__ __forceinline__ double pow2_inverse(float m) {
+__device__ __forceinline__ float pow2_inverse(float m) {
     // 2^-e with e the binary exponent of m (exact scaling); 1 for 0/inf/nan
-    if (!(m > 0.f) || !(m < 3.0e38f)) return 1.0;
-    return ldexp(1.0, -ilogbf(m));
+    if (!(m > 0.f) || !(m < 3.0e38f)) return 1.f;
+    return ldexpf(1.f, -ilogbf(m));
 }
 
-// Mixed: LU32 = Dr (c I - J32) Dc with power-of-two row and column
-// equilibration (Dr, Dc kept in s.dr / s.dc for the solves).
+// Mixed: LU32 = Dr (c I - J64) Dc in FP32 with power-of-two row and column
+// equilibration (Dr, Dc kept in s.dr / s.dc, as doubles, for the solves).
+// One narrowing per element; the equilibration runs on the FP32 pipe.
 template<int G>
 __device__ __noinline__ void form_iteration_matrix_scaled(const Grp<G>& g, const Slot<float>& s, int n,
                                                           double c) {
     const int ld = s.ld;
+    float* LU = s.LU;
+    // pass 1: narrow -J to FP32 (the diagonal in FP64 first), row maxima
     for (int i = g.rank; i < n; i += G) {
-        const float* row = s.J + (size_t)i * ld;
+        const double* Ji = s.J64 + (size_t)i * ld;
+        float* Li = LU + (size_t)i * ld;
         float mx = 0.f;
         for (int j = 0; j < n; j++) {
-            const float a = (i == j) ? float(c - double(row[j])) : -row[j];
+            const float a = (j == i) ? float(c - Ji[j]) : -float(Ji[j]);
+            Li[j] = a;
             mx = fmaxf(mx, fabsf(a));
         }
-        s.dr[i] = pow2_inverse(mx);
+        s.dr[i] = double(pow2_inverse(mx));
     }
     g.sync();
+    // pass 2: column maxima of the row-scaled matrix
     for (int j = g.rank; j < n; j += G) {
         float mx = 0.f;
-        for (int i = 0; i < n; i++) {
-            const float jv = s.J[(size_t)i * ld + j];
-            const float a = (i == j) ? float(c - double(jv)) : -jv;
-            mx = fmaxf(mx, fabsf(a * float(s.dr[i])));
-        }
-        s.dc[j] = pow2_inverse(mx);
+        for (int i = 0; i < n; i++) mx = fmaxf(mx, fabsf(LU[(size_t)i * ld + j] * float(s.dr[i])));
+        s.dc[j] = double(pow2_inverse(mx));
     }
     g.sync();
-    for (int idx = g.rank; idx < n * ld; idx += G) {
-        const int i = idx / ld, j = idx - i * ld;
-        if (j >= n) continue;
-        const float jv = s.J[idx];
-        const float a = (i == j) ? float(c - double(jv)) : -jv;
-        s.LU[idx] = a * float(s.dr[i]) * float(s.dc[j]);
+    // pass 3: apply both scalings (exact: powers of two)
+    for (int i = g.rank; i < n; i += G) {
+        float* Li = LU + (size_t)i * ld;
+        const float ri = float(s.dr[i]);
+        for (int j = 0; j < n; j++) Li[j] = Li[j] * ri * float(s.dc[j]);
     }
     g.sync();
 }
 
-// Mixed solve: x0 = Dc LU32^-1 Dr b (FP32), r = b - (c x0 - J32 x0) in FP64,
-// x = x0 + Dc LU32^-1 Dr r.  Returns false when the correction is not small
-// (or not finite): the caller then repeats the work in FP64.
+// Mixed solve: x0 = Dc LU32^-1 Dr b (FP32 vectors), r = b - (c x0 - J64 x0)
+// in FP64, x = x0 + Dc LU32^-1 Dr r.  Returns false when the correction is
+// not small (or not finite): the caller then repeats the work in FP64.
 template<int G>
 __device__ __noinline__ bool linear_solve_mixed(const Grp<G>& g, const DevMech& M, const Slot<float>& s,
                                                 double c, double* b, double* tmp) {
     const int n = M.n, ld = s.ld;
-    for (int i = g.rank; i < n; i += G) {
-        tmp[i] = b[i];
-        b[i] = b[i] * s.dr[i];
-    }
-    g.sync();
-    lu_solve<G, float>(g, s.LU, n, ld, s.piv, s.invD, b);
-    for (int i = g.rank; i < n; i += G) b[i] = b[i] * s.dc[i];
+    for (int i = g.rank; i < n; i += G) s.x32[i] = float(b[i] * s.dr[i]);
+    lu_solve<G, float, float>(g, s.LU, n, ld, s.piv, s.invD, s.x32);
+    for (int i = g.rank; i < n; i += G) tmp[i] = double(s.x32[i]) * s.dc[i];
     g.sync();
     for (int i = g.rank; i < n; i += G) {
-        const float* Ji = s.J + (size_t)i * ld;
-        double r = tmp[i] - c * b[i];
-        for (int j = 0; j < n; j++) r = fma(double(Ji[j]), b[j], r);
-        tmp[i] = r * s.dr[i];
+        const double* Ji = s.J64 + (size_t)i * ld;
+        double r = b[i] - c * tmp[i];
+        for (int j = 0; j < n; j++) r = fma(Ji[j], tmp[j], r);
+        s.r32[i] = float(r * s.dr[i]);
     }
-    g.sync();
-    lu_solve<G, float>(g, s.LU, n, ld, s.piv, s.invD, tmp);
+    lu_solve<G, float, float>(g, s.LU, n, ld, s.piv, s.invD, s.r32);
     double dmax = 0, xmax = 0;
     for (int i = g.rank; i < n; i += G) {
-        const double d = tmp[i] * s.dc[i];
-        const double x = b[i] + d;
+        const double d = double(s.r32[i]) * s.dc[i];
+        const double x = tmp[i] + d;
         b[i] = x;
         const double ad = fabs(d), ax = fabs(x);
         dmax = (ad > dmax || ad != ad) ? ad : dmax;
@@ -157,7 +129,6 @@ template<int G, class MT>
 __device__ __forceinline__ void jacobian_into(const Grp<G>& g, const DevMech& M, const Slot<MT>& s,
                                               const Slot<double>& sd, double p, double* y, double* f, int fast) {
     jac_eval<G, double>(g, M, sd, p, y, f, sd.J, fast);
-    if constexpr (sizeof(MT) == 4) jac_to_fp32<G>(g, sd.J, s.J, M.n * s.ld);
 }
 
 template<int G, class MT>
@@ -171,7 +142,7 @@ template<int G, class MT>
 __device__ __forceinline__ bool stage_solve(const Grp<G>& g, const DevMech& M, const Slot<MT>& s, double c,
                                             double* b, double* tmp) {
     if constexpr (sizeof(MT) == 8) {
-        lu_solve<G, double>(g, s.LU, M.n, s.ld, s.piv, s.invD, b);
+        lu_solve<G, double, double>(g, s.LU, M.n, s.ld, s.piv, s.invD, b);
         return true;
     } else {
         return linear_solve_mixed<G>(g, M, s, c, b, tmp);

@@ -54,7 +54,8 @@ class StepStats(C.Structure):
                 ("cells_failed", C.c_int64), ("attempts", C.c_int64), ("accepted", C.c_int64),
                 ("jacobians", C.c_int64), ("lu_decompositions", C.c_int64),
                 ("rhs_evaluations", C.c_int64), ("linear_solves", C.c_int64),
-                ("fp64_fallbacks", C.c_int64), ("kernel_ms", C.c_double), ("call_ms", C.c_double)]
+                ("fp64_fallbacks", C.c_int64), ("kernel_ms", C.c_double), ("call_ms", C.c_double),
+                ("mapping", C.c_int32), ("reserved", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

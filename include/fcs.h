@@ -157,6 +157,8 @@ typedef struct fcs_step_stats {
     double  kernel_ms;           /* device time of the integration kernel */
     double  call_ms;             /* device time of the whole call on the library's
                                     stream, host<->device copies included */
+    int32_t mapping;             /* threads per cell used (autotuned for AUTO) */
+    int32_t reserved;
 } fcs_step_stats;
 
 fcs_status fcs_create(fcs_ctx** ctx, int device);
