@@ -17,78 +17,20 @@
 #include "fcs_device.cuh"
 #include "fcs_internal.h"
 #include "fcs_launch.h"
+#include "fcs_ctx.h"
 
 using namespace fcs;
 
-namespace {
 
-template<class T>
-struct DBuf {
-    T* p = nullptr;
-    size_t n = 0;
-    cudaError_t ensure(size_t want) {
-        if (want <= n) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-        cudaError_t e = cudaMalloc(&p, std::max<size_t>(want, 1) * sizeof(T));
-        if (e == cudaSuccess) n = want;
-        return e;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-};
-
-struct Shape {
-    LaunchCfg lc;
-    SlotLayout L;
-    bool global;      // workspace in global memory
-    bool mixed;
-};
-
-}  // namespace
-
-struct fcs_ctx {
-    int device = 0;
-    int numSMs = 0;
-    size_t maxSmemPerBlock = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evc0 = nullptr, evc1 = nullptr;
-    std::string err;
-    // mechanism
-    bool loaded = false;
-    DevMech M{};
-    DBuf<double> dW, dInvW, dTc, dCoef, dEff, dPlogRow, dPlogTa, dHf;
-    DBuf<RxnInfo> dRx;
-    DBuf<int> dPlogOff, dIncOff, dInc, dTbInc;
-    // options
-    fcs_options opt{};
-    // per-call buffers
-    DBuf<double> bp, brho, bT, bY, bSub, bRR, bDt, bOut, bJ, bQ;
-    DBuf<int> bStatus, bOrder, bHead;
-    DBuf<long long> bStats;
-    DBuf<unsigned long long> bMin;
-    DBuf<char> gws;
-    std::map<std::tuple<int, int, int, int>, int> tuned;  // (n, precision, solver, jac) -> group
-};
-
-static fcs_status set_err(fcs_ctx* c, fcs_status s, const std::string& m) {
+fcs_status fcs::set_err(fcs_ctx* c, fcs_status s, const std::string& m) {
     if (c) c->err = m;
     return s;
 }
 
-static fcs_status cuda_err(fcs_ctx* c, cudaError_t e, const char* where) {
+fcs_status fcs::cuda_err(fcs_ctx* c, cudaError_t e, const char* where) {
     return set_err(c, FCS_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
-#define CK(call)                                                  \
-    do {                                                          \
-        cudaError_t e_ = (call);                                  \
-        if (e_ != cudaSuccess) return cuda_err(ctx, e_, #call);   \
-    } while (0)
 
 extern "C" const char* fcs_version(void) { return "fcs-gb300 1.0 (sm_103a)"; }
 
@@ -326,7 +268,7 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
 // ------------------------------------------------------------------------
 // launch shapes
 
-static KOpts kopts(const fcs_options& o) {
+KOpts fcs::kopts(const fcs_options& o) {
     KOpts k;
     k.solver = o.solver;
     k.jacobian = o.jacobian;
@@ -340,7 +282,7 @@ static KOpts kopts(const fcs_options& o) {
 }
 
 // Build the launch shape for a group size; returns false when impossible.
-static bool make_shape(fcs_ctx* ctx, int group, bool integrate, Shape& sh) {
+bool fcs::make_shape(fcs_ctx* ctx, int group, bool integrate, Shape& sh) {
     const fcs_options& o = ctx->opt;
     const bool mixed = o.precision == FCS_PRECISION_MIXED;
     const bool seulex = integrate && o.solver == FCS_SOLVER_SEULEX;
@@ -381,7 +323,7 @@ static fcs_status ensure_gws(fcs_ctx* ctx, const Shape& sh) {
     return FCS_OK;
 }
 
-static int default_group(fcs_ctx* ctx) {
+int fcs::default_group(fcs_ctx* ctx) {
     const int n = ctx->M.n;
     if (n <= 128) return 64;
     return 128;

@@ -1,0 +1,87 @@
+// fcs_ctx.h -- the context object behind the opaque fcs_ctx handle and the
+// host-side helpers shared by the C ABI translation units (fcs_capi.cu,
+// fcs_noalloc.cu).  Internal: not part of the public headers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <map>
+#include <string>
+#include <tuple>
+
+#include "../../include/fcs.h"
+#include "fcs_device.cuh"
+#include "fcs_internal.h"
+#include "fcs_launch.h"
+
+namespace fcs {
+
+template<class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t ensure(size_t want) {
+        if (want <= n) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(want, 1) * sizeof(T));
+        if (e == cudaSuccess) n = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct Shape {
+    LaunchCfg lc;
+    SlotLayout L;
+    bool global;      // workspace in global memory
+    bool mixed;
+};
+
+}  // namespace fcs
+
+struct fcs_ctx {
+    int device = 0;
+    int numSMs = 0;
+    size_t maxSmemPerBlock = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evc0 = nullptr, evc1 = nullptr;
+    std::string err;
+    // mechanism
+    bool loaded = false;
+    fcs::DevMech M{};
+    fcs::DBuf<double> dW, dInvW, dTc, dCoef, dEff, dPlogRow, dPlogTa, dHf;
+    fcs::DBuf<fcs::RxnInfo> dRx;
+    fcs::DBuf<int> dPlogOff, dIncOff, dInc, dTbInc;
+    // options
+    fcs_options opt{};
+    // per-call buffers
+    fcs::DBuf<double> bp, brho, bT, bY, bSub, bRR, bDt, bOut, bJ, bQ;
+    fcs::DBuf<int> bStatus, bOrder, bHead;
+    fcs::DBuf<long long> bStats;
+    fcs::DBuf<unsigned long long> bMin;
+    fcs::DBuf<char> gws;
+    std::map<std::tuple<int, int, int, int>, int> tuned;  // (n, precision, solver, jac) -> group
+};
+
+namespace fcs {
+
+fcs_status set_err(fcs_ctx* c, fcs_status s, const std::string& m);
+fcs_status cuda_err(fcs_ctx* c, cudaError_t e, const char* where);
+KOpts kopts(const fcs_options& o);
+// Launch shape for a group size; false when impossible.
+bool make_shape(fcs_ctx* ctx, int group, bool integrate, Shape& sh);
+int default_group(fcs_ctx* ctx);
+
+}  // namespace fcs
+
+#define CK(call)                                                       \
+    do {                                                               \
+        cudaError_t e_ = (call);                                       \
+        if (e_ != cudaSuccess) return fcs::cuda_err(ctx, e_, #call);   \
+    } while (0)

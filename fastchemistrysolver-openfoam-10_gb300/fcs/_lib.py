@@ -27,7 +27,8 @@ ERRORS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "STATE", 5: "CELLS", 
 
 EXPORTS = ("fcs_create", "fcs_destroy", "fcs_last_error_string", "fcs_version", "fcs_load_mechanism",
            "fcs_load_mechanism_foam", "fcs_read_chemistry_properties", "fcs_default_options",
-           "fcs_set_options", "fcs_mechanism_size", "fcs_integrate", "fcs_integrate_lts", "fcs_rhs",
+           "fcs_set_options", "fcs_mechanism_size", "fcs_integrate", "fcs_integrate_lts",
+           "fcs_integrate_noalloc", "fcs_rhs",
            "fcs_jacobian", "fcs_rates", "fcs_bench_fp64_peak", "fcs_bench_fp32_peak", "fcs_check_exp")
 
 
@@ -87,6 +88,7 @@ def load(path: str = LIB) -> C.CDLL:
     cell_args = [vp, C.c_int64, C.c_double, vp, vp, vp, vp, vp, vp, vp, C.POINTER(StepStats), _dp, C.c_int32]
     L.fcs_integrate.argtypes = cell_args
     L.fcs_integrate_lts.argtypes = [vp, C.c_int64, vp] + cell_args[3:]
+    L.fcs_integrate_noalloc.argtypes = cell_args[:-1]
     L.fcs_rhs.argtypes = [vp, C.c_int64, vp, vp, vp, vp, C.c_int32]
     L.fcs_jacobian.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, C.c_int32]
     L.fcs_rates.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, vp, C.c_int32]
@@ -244,6 +246,19 @@ class Context:
         if check and st not in (0, 5):
             self._check(st)
         return st, stats.as_dict(), dmin.value
+
+    def integrate_noalloc(self, n, dt, p, rho0, T, Y, sub, RR=None, status=None, check=True):
+        """fcs_integrate_noalloc on caller-owned device arrays (torch CUDA tensors)."""
+        stats = StepStats()
+        dmin = C.c_double(0)
+        st = self.L.fcs_integrate_noalloc(self.h, n, dt, _addr(p), _addr(rho0), _addr(T), _addr(Y), _addr(sub),
+                                          _addr(RR), _addr(status), C.byref(stats), C.byref(dmin))
+        if check and st not in (0, 5):
+            self._check(st)
+        return st, stats.as_dict(), dmin.value
+
+    def last_error(self):
+        return self.L.fcs_last_error_string(self.h).decode()
 
     def integrate(self, cells, dt, dt_per_cell=None):
         """Integrate a copy of host ``cells``; returns the same dict as the oracle."""

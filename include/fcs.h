@@ -219,6 +219,45 @@ fcs_status fcs_integrate_lts(fcs_ctx* ctx, int64_t n_cells, const double* delta_
                              int32_t flags);
 
 /*
+ * fcs_integrate_noalloc -- no counterpart in the reference.
+ *
+ * fcs_integrate over caller-owned DEVICE arrays that allocates no device
+ * memory: no cudaMalloc/cudaFree and no allocating library routine, on any
+ * call.  For callers that cannot allocate during a time step: a flow solver
+ * that gives all free device memory to its own pool at start-up, and one
+ * whose other streams must not be stalled by the device-wide synchronisation
+ * of cudaMalloc/cudaFree when fcs_integrate's grow-only buffers grow.
+ *
+ * Same arguments and results as fcs_integrate with FCS_PTR_DEVICE (p, rho0,
+ * T, Y, sub_delta_t, RR, cell_status are device or managed memory of the
+ * context's device; stats and delta_t_min are host).  The step counters,
+ * minimum sub-step, work-queue head and queue of reacting cells live in one
+ * fixed device array of this library, per device, so:
+ *   - n_cells is at most FCS_NOALLOC_MAX_CELLS (4 MiB of queue); larger
+ *     calls return FCS_ERR_INVALID without doing anything;
+ *   - the per-cell workspace must fit in shared memory (about 140 species
+ *     for the Rosenbrock solvers in FP64, 120 mixed, 100 for Seulex, with
+ *     about seven reactions per species); otherwise FCS_ERR_UNSUPPORTED;
+ *   - the call zeroes the counters and queue head itself before its kernels;
+ *     nothing has to be cleared by the caller;
+ *   - calls that overlap in time on the same device (two host threads, or two
+ *     contexts) race on that array and must be serialised by the caller;
+ *     consecutive calls from one thread are safe (each call returns after its
+ *     work has finished);
+ *   - the mapping autotuner is not run (it allocates trial copies): the
+ *     mapping is fcs_options.mapping, else one the autotuner already cached in
+ *     this context, else the default for the mechanism size;
+ *   - the first call on a device looks up the array's address (which may load
+ *     this library's device code); make it before any stream capture begins.
+ */
+#define FCS_NOALLOC_MAX_CELLS 1048576
+fcs_status fcs_integrate_noalloc(fcs_ctx* ctx, int64_t n_cells, double delta_t,
+                                 const double* p, const double* rho0,
+                                 double* T, double* Y, double* sub_delta_t,
+                                 double* RR, int32_t* cell_status,
+                                 fcs_step_stats* stats, double* delta_t_min);
+
+/*
  * Right-hand side of the mass-fraction ODE system at each cell state:
  * dydt[(Ns+1)*n] (species-major, row Ns is dT/dt).  Mirrors
  * FastChemistryModel::derivatives (FastChemistryModel.C:194-273) on top of
