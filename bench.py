@@ -5,7 +5,16 @@ Workload (default): ``counterflow_53s`` -- the 53-species / 325-reaction
 synthetic mechanism with 20 PLOG reactions, 65,536 cells on a 256 x 256
 counterflow-like field, one CFD step dt = 1e-6 s integrated by OptRodas34
 (absTol 1e-8, relTol 1e-4, exact Jacobian, initial sub-step 1e-7).  A step is
-one call of the batched solve over all cells from the same initial state.
+one call of the batched solve over all cells from the same initial state;
+the plain method runs it as one CUDA graph (classify, binned work queue,
+persistent integrator).
+
+* gated : the same cells through the surrogate-gated method (an MLP ensemble
+          trained before timing on ``--train-samples`` other cells of the same
+          kind, integrated by the plain method), with its fallback rate and
+          audit errors
+* accuracy : both methods against the same integrator at absTol 1e-14 /
+          relTol 1e-10 on a sample of cells
 
 * value : cells / device time of the step with inputs resident in HBM
           (CUDA events on the library's launching stream; the reset of the
@@ -23,6 +32,7 @@ the reference's own AVX2 core does not build on the aarch64 GPU hosts) on the
 host cores with the same metric.
 """
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -53,6 +63,12 @@ def parse():
     ap.add_argument("--cells", type=int, default=0, help="0: the workload's full cell count")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--method", default="both", choices=["plain", "gated", "both"],
+                    help="plain GPU method, the surrogate-gated method, or both on the same cells")
+    ap.add_argument("--train-samples", type=int, default=65536,
+                    help="cells integrated by the plain method to train the surrogate (before timing)")
+    ap.add_argument("--accuracy-cells", type=int, default=256,
+                    help="cells checked against a tight-tolerance run (0: skip)")
     return ap.parse_args()
 
 
@@ -201,6 +217,44 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def device_state(cells, dev):
+    import torch
+    return {k: torch.from_numpy(np.ascontiguousarray(getattr(cells, k))).to(dev)
+            for k in ("p", "rho0", "T", "Y", "subDt")}
+
+
+def accuracy(ctx, w, cells, idx, results, dev):
+    """Max relative T and absolute Y error of each result on cells `idx`
+    against the same GPU FP64 integrator at absTol 1e-14 / relTol 1e-10 (the
+    FP64 oracle tolerances; the integrator is parity-tested against the
+    reference)."""
+    import torch
+    o = ctx.options
+    sub = cells.subset(idx)
+    d = device_state(sub, dev)
+    ctx.set_options(solver=args_solver(o), jacobian="exact", precision="fp64", mapping=o.mapping,
+                    abs_tol=1e-14, rel_tol=1e-10, max_steps=10 ** 7, treact=o.T_react)
+    st = torch.zeros(sub.n, dtype=torch.int32, device=dev)
+    ctx.integrate_raw(sub.n, w.dt, d["p"], d["rho0"], d["T"], d["Y"], d["subDt"], None, st, device=True)
+    ctx.options = o
+    ctx._check(ctx.L.fcs_set_options(ctx.h, ctypes.byref(o)))
+    Tt, Yt = d["T"].cpu().numpy(), d["Y"].cpu().numpy()
+    act = sub.T > o.T_react
+    out = {}
+    for name, (T, Y) in results.items():
+        eT = np.abs(T[idx] - Tt) / Tt
+        eY = np.abs(Y[:, idx] - Yt).max(axis=0)
+        out[name] = {"max_rel_T": float(eT[act].max()) if act.any() else 0.0,
+                     "p99_rel_T": float(np.percentile(eT[act], 99)) if act.any() else 0.0,
+                     "max_abs_Y": float(eY[act].max()) if act.any() else 0.0}
+    return out
+
+
+def args_solver(o):
+    from fcs import _lib
+    return {v: k for k, v in _lib.SOLVERS.items()}[o.solver]
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -212,7 +266,7 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     import fcs
-    from fcs import _lib
+    from fcs import _lib, surrogate
     w = fcs.WORKLOADS[args.workload]
     mech = w.mechanism()
     flat = fcs.flatten(mech)
@@ -224,67 +278,136 @@ def main():
                     abs_tol=w.abs_tol, rel_tol=w.rel_tol, treact=w.treact)
     dev = torch.device("cuda", local)
     # pristine inputs resident in HBM, and working buffers
-    P = {k: torch.from_numpy(np.ascontiguousarray(getattr(cells, k))).to(dev) for k in ("p", "rho0", "T", "Y", "subDt")}
+    P = device_state(cells, dev)
     T = P["T"].clone(); Y = P["Y"].clone(); S = P["subDt"].clone()
     RR = torch.zeros_like(Y)
     st = torch.zeros(n, dtype=torch.int32, device=dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
+    gated = args.method in ("gated", "both")
+    plain = args.method in ("plain", "both")
 
-    def step():
+    def reset():
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         T.copy_(P["T"]); Y.copy_(P["Y"]); S.copy_(P["subDt"])
         e1.record()
         torch.cuda.synchronize()
-        code, stats, dmin = ctx.integrate_raw(n, w.dt, P["p"], P["rho0"], T, Y, S, RR, st, device=True)
-        return e0.elapsed_time(e1) + stats["call_ms"], stats
+        return e0.elapsed_time(e1)
 
-    for _ in range(args.warmup):
-        step()
-    peak64 = _lib.fp64_peak_tflops(local)
-    times, kms, all_stats = [], [], []
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
+    def step_plain(graph=True):
+        ms = reset()
+        code, stats, dmin = ctx.integrate_raw(n, w.dt, P["p"], P["rho0"], T, Y, S, RR, st, device=True,
+                                              flags=_lib.CUDA_GRAPH if graph else 0)
+        return ms + stats["call_ms"], stats
+
+    def step_gated():
+        ms = reset()
+        code, stats, gst, dmin = _lib.integrate_gated_raw(ctx, n, w.dt, P["p"], P["rho0"], T, Y, S, RR, st,
+                                                          device=True)
+        return ms + stats["call_ms"], stats, gst
+
+    def timed(fn):
+        times, out = [], []
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
         for _ in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
-            ms, stats = step()
-            times.append(ms)
-            kms.append(stats["kernel_ms"])
-            all_stats.append(stats)
-    torch.cuda.synchronize()
-    t_step = statistics.mean(times)
-    if ws > 1:
-        t = torch.tensor([t_step], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(t.item())
-        torch.distributed.barrier()
+            r = fn()
+            times.append(r[0])
+            out.append(r)
+        torch.cuda.synchronize()
+        t = statistics.mean(times)
+        if ws > 1:
+            tt = torch.tensor([t], device=dev)
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            t = float(tt.item())
+        return t, out
+
+    # the first call autotunes the cell-to-thread mapping (outside the graph)
+    step_plain(graph=False)
+    for _ in range(args.warmup):
+        step_plain()
+    peak64 = _lib.fp64_peak_tflops(local)
+    with ClockSampler(local) as clk:
+        t_step, outs = timed(step_plain)
+    T_plain, Y_plain = T.cpu().numpy(), Y.cpu().numpy()
     value = ws * n / (t_step * 1e-3)
-    s0 = all_stats[-1]
+    s0 = outs[-1][1]
+    kms = [o[1]["kernel_ms"] for o in outs]
     # e2e through the C ABI with pinned host buffers
     hp = {k: torch.from_numpy(np.ascontiguousarray(getattr(cells, k))).pin_memory() for k in ("p", "rho0", "T", "Y", "subDt")}
     hT, hY, hS = hp["T"].clone().pin_memory(), hp["Y"].clone().pin_memory(), hp["subDt"].clone().pin_memory()
     hRR = torch.zeros_like(hY).pin_memory()
     hst = torch.zeros(n, dtype=torch.int32).pin_memory()
     e2e_ms = []
-    e2e_warm = 1  # the device path above is already warm
-    for i in range(e2e_warm + args.steps):
+    for i in range(1 + args.steps):
         hT.copy_(hp["T"]); hY.copy_(hp["Y"]); hS.copy_(hp["subDt"])
         flush.zero_()
         torch.cuda.synchronize()
         code, stats, dmin = ctx.integrate_raw(n, w.dt, hp["p"].numpy(), hp["rho0"].numpy(), hT.numpy(), hY.numpy(),
                                               hS.numpy(), hRR.numpy(), hst.numpy())
-        if i >= e2e_warm:
+        if i >= 1:
             e2e_ms.append(stats["call_ms"])
     t_e2e = statistics.mean(e2e_ms)
     if ws > 1:
-        t = torch.tensor([t_e2e], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(t.item())
+        tt = torch.tensor([t_e2e], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(tt.item())
     h2d = 8 * n * (4 + ns)
     d2h = 8 * n * (2 + 2 * ns) + 4 * n
+    # the surrogate-gated method on the same cells
+    gated_line = None
+    results = {"plain": (T_plain, Y_plain)}
+    if gated:
+        mlp, info = surrogate.train_for_workload(ctx, w, mech, args.train_samples, seed=1000 + rank)
+        surrogate.attach(ctx, mlp, mech)
+        for _ in range(args.warmup):
+            step_gated()
+        t_g, gouts = timed(step_gated)
+        results["gated"] = (T.cpu().numpy(), Y.cpu().numpy())
+        sg, gg = gouts[-1][1], gouts[-1][2]
+        # the tensor-core MLP alone: one ensemble forward over the field
+        x = torch.from_numpy(surrogate.features(cells.T, cells.p, w.dt, cells.Y)).to(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        mlp.forward(0, x, device=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for m in range(mlp.members):
+            mlp.forward(m, x, device=True)
+        e1.record()
+        torch.cuda.synchronize()
+        mlp_ms = e0.elapsed_time(e1)
+        dims = [ns + 3] + [mlp.width] * mlp.depth + [ns + 2]
+        mlp_flop = 2.0 * n * mlp.members * sum(dims[i] * dims[i + 1] for i in range(len(dims) - 1))
+        peaks = {}
+        try:
+            with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+                peaks = json.load(f)
+        except OSError:
+            pass
+        bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
+        gated_line = {"value": ws * n / (t_g * 1e-3), "unit": "cells/s", "ms_per_step": t_g,
+                      "cells_active": gg["cells_active"], "cells_accepted": gg["cells_accepted"],
+                      "cells_fallback": gg["cells_fallback"], "cells_audited": gg["cells_audited"],
+                      "fallback_rate": gg["cells_fallback"] / max(1, gg["cells_active"]),
+                      "audit_max_rel_T": gg["audit_max_rel_T"], "audit_max_abs_Y": gg["audit_max_abs_Y"],
+                      "surrogate_ms": gg["surrogate_ms"], "integrate_ms": gg["integrate_ms"],
+                      "attempts": sg["attempts"], "training": info,
+                      "mlp_roofline": {"bound": "tensor", "achieved": mlp_flop / (mlp_ms * 1e-3) / 1e12,
+                                       "peak": bf16_peak, "unit": "TFLOP/s",
+                                       "frac": mlp_flop / (mlp_ms * 1e-3) / 1e12 / bf16_peak,
+                                       "ms_ensemble_forward": mlp_ms,
+                                       "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst)"}}
+        _lib.attach_surrogate(ctx, None)
+    acc = None
+    if args.accuracy_cells > 0:
+        rng = np.random.default_rng(5)
+        idx = np.sort(rng.choice(n, min(n, args.accuracy_cells), replace=False))
+        acc = accuracy(ctx, w, cells, idx, results, dev)
+        acc["reference"] = "GPU FP64 integrator at absTol 1e-14, relTol 1e-10, maxSteps 1e7 on the sampled cells"
+        acc["cells"] = int(idx.size)
     # roofline of the integrator kernel
     f64, f32, n_exp = flops_per_attempt(ns, mech.n_reactions, mech.count(1), mech.count(2), args.solver,
                                         args.precision)
@@ -307,20 +430,25 @@ def main():
             "data": "synthetic (seeded generator, no dataset)",
             "config": {"workload": w.name, "cells": n, "species": ns, "reactions": mech.n_reactions,
                        "solver": args.solver, "precision": args.precision, "jacobian": w.jacobian,
-                       "dt": w.dt, "abs_tol": w.abs_tol, "rel_tol": w.rel_tol,
+                       "dt": w.dt, "abs_tol": w.abs_tol, "rel_tol": w.rel_tol, "method": "plain GPU " + args.solver,
+                       "step": "one CUDA graph per step (classify, binned work queue, persistent integrator)",
                        "l2": "flushed (256 MB write) before every timed step",
                        "parallelism": f"replicas x{ws} (cells independent, no collective)"},
             "e2e": {"value": ws * n / (t_e2e * 1e-3), "unit": "cells/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": 2 * args.steps,
+            "gpu_launches": 3 * args.steps,  # classify_bin_kernel, queue_kernel, integrate_kernel
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
                          "frac": achieved / peak64, "traffic": traffic,
                          "peak_source": "measured: dense FP64 FMA chains on this GPU (fcs_bench_fp64_peak)",
                          "flops_per_attempt_fp64": f64, "flops_per_attempt_fp32": f32,
                          "transcendentals_per_attempt": n_exp, "kernel_ms": k_ms},
-            "stats": {k: s0[k] for k in ("cells_integrated", "cells_failed", "attempts", "accepted",
-                                         "jacobians", "rhs_evaluations", "fp64_fallbacks")},
+            "stats": {k: s0[k] for k in ("cells_integrated", "cells_skipped", "cells_failed", "attempts", "accepted",
+                                         "jacobians", "rhs_evaluations", "fp64_fallbacks", "mapping")},
             "clocks": clk.summary()}
+    if gated_line:
+        line["gated"] = gated_line
+    if acc:
+        line["accuracy"] = acc
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rate, done, tu = cpu_baseline(flat, w, cells, args.cpu_seconds, threads)

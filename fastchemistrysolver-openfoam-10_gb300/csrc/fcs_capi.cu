@@ -76,6 +76,7 @@ extern "C" fcs_status fcs_destroy(fcs_ctx* ctx) {
     if (!ctx) return FCS_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    gate_release(ctx);
     for (DBuf<double>* b : {&ctx->dW, &ctx->dInvW, &ctx->dTc, &ctx->dCoef, &ctx->dEff, &ctx->dPlogRow,
                             &ctx->dPlogTa, &ctx->dHf, &ctx->bp, &ctx->brho, &ctx->bT, &ctx->bY,
                             &ctx->bSub, &ctx->bRR, &ctx->bDt, &ctx->bOut, &ctx->bJ, &ctx->bQ})
@@ -83,7 +84,9 @@ extern "C" fcs_status fcs_destroy(fcs_ctx* ctx) {
     ctx->dRx.release();
     ctx->dPlogOff.release(); ctx->dIncOff.release(); ctx->dInc.release(); ctx->dTbInc.release();
     ctx->bStatus.release(); ctx->bOrder.release(); ctx->bHead.release();
-    ctx->bStats.release(); ctx->bMin.release(); ctx->gws.release();
+    ctx->bStats.release(); ctx->bMin.release(); ctx->gws.release(); ctx->bBin.release();
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    if (ctx->hStats) cudaFreeHost(ctx->hStats);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->evc0) cudaEventDestroy(ctx->evc0);
@@ -421,35 +424,102 @@ static fcs_status integrate_impl(fcs_ctx* ctx, int64_t nc, double dt, const doub
         io.subDt = ctx->bSub.p; io.RR = RR ? ctx->bRR.p : nullptr; io.status = ctx->bStatus.p;
         io.dtPerCell = dtc ? ctx->bDt.p : nullptr;
     }
+    const bool sorted = !(flags & FCS_NO_QUEUE_SORT);
+    const bool graph = flags & FCS_CUDA_GRAPH;
+    if (graph && !dev) return set_err(ctx, FCS_ERR_INVALID, "FCS_CUDA_GRAPH needs FCS_PTR_DEVICE");
     CK(ctx->bStats.ensure(ST_COUNT));
     CK(ctx->bMin.ensure(1));
     CK(ctx->bOrder.ensure(std::max<int64_t>(nc, 1)));
-    CK(ctx->bHead.ensure(2));
+    CK(ctx->bHead.ensure(QC_COUNT));  // head, length and the bin counters of the queue
+    if (sorted) CK(ctx->bBin.ensure(std::max<int64_t>(nc, 1)));
     io.stats = ctx->bStats.p;
     io.dtMinBits = ctx->bMin.p;
-    CK(cudaMemsetAsync(ctx->bStats.p, 0, ST_COUNT * sizeof(long long), st));
-    CK(cudaMemsetAsync(ctx->bMin.p, 0x7f, sizeof(unsigned long long), st));
-    CK(cudaMemsetAsync(ctx->bHead.p, 0, 2 * sizeof(int), st));
-    // classify: cells with T <= Treact are skipped (transientSolve.H:39, 70-76)
-    CK(launch_classify(io, ns, ctx->opt.T_react, ctx->bOrder.p, ctx->bHead.p + 1, st));
-    int nActive = 0;
-    CK(cudaMemcpyAsync(&nActive, ctx->bHead.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    const int group = ctx->opt.mapping ? ctx->opt.mapping : tuned_group(ctx, io, nActive);
-    Shape sh;
-    if (!make_shape(ctx, group, true, sh))
-        return set_err(ctx, FCS_ERR_UNSUPPORTED, "no launch shape for this mapping");
-    fcs_status s = ensure_gws(ctx, sh);
-    if (s != FCS_OK) return s;
-    WorkQueue q{ctx->bHead.p, ctx->bOrder.p, nActive};
     const KOpts ko = kopts(ctx->opt);
-    CK(cudaEventRecord(ctx->ev0, st));
-    if (nActive > 0) CK(launch_integrate(sh.lc, sh.mixed, ctx->M, ko, sh.L, io, q, sh.global ? ctx->gws.p : nullptr, st));
-    CK(cudaEventRecord(ctx->ev1, st));
-    long long hs[ST_COUNT];
-    unsigned long long hmin = 0;
-    CK(cudaMemcpyAsync(hs, ctx->bStats.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(&hmin, ctx->bMin.p, sizeof(hmin), cudaMemcpyDeviceToHost, st));
+    // The step's device work: counters, classify (cells with T <= Treact are
+    // skipped, transientSolve.H:39, 70-76), the queue ordered by predicted
+    // step count, and the persistent integrator reading the queue length on
+    // the device.
+    auto enqueue_prologue = [&]() -> cudaError_t {
+        cudaError_t e;
+        if ((e = cudaMemsetAsync(ctx->bStats.p, 0, ST_COUNT * sizeof(long long), st)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(ctx->bMin.p, 0x7f, sizeof(unsigned long long), st)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(ctx->bHead.p, 0, QC_COUNT * sizeof(int), st)) != cudaSuccess) return e;
+        if (!sorted) return launch_classify(io, ns, ctx->opt.T_react, ctx->bOrder.p, ctx->bHead.p + QC_LEN, st);
+        if ((e = launch_classify_binned(io, ns, ctx->opt.T_react, ctx->bBin.p, ctx->bHead.p, st)) != cudaSuccess)
+            return e;
+        return launch_queue(nc, ctx->bBin.p, ctx->bHead.p, ctx->bOrder.p, st);
+    };
+    long long* hs = ctx->hStats;
+    unsigned long long hminv = 0;
+    unsigned long long* hmin = &hminv;
+    long long hsLocal[ST_COUNT];
+    int group = 0;
+    if (graph) {
+        // one CUDA graph per step shape: replayed while the arrays, sizes and
+        // options stay the same, re-captured when any of them changes
+        if (!ctx->hStats) CK(cudaMallocHost(&ctx->hStats, (ST_COUNT + 1) * sizeof(long long)));
+        hs = ctx->hStats;
+        hmin = reinterpret_cast<unsigned long long*>(ctx->hStats + ST_COUNT);
+        group = ctx->opt.mapping ? ctx->opt.mapping : [&] {
+            const auto it = ctx->tuned.find(std::make_tuple(ctx->M.n, (int)ctx->opt.precision, (int)ctx->opt.solver,
+                                                            (int)ctx->opt.jacobian));
+            return it != ctx->tuned.end() ? it->second : default_group(ctx);
+        }();
+        Shape sh;
+        if (!make_shape(ctx, group, true, sh))
+            return set_err(ctx, FCS_ERR_UNSUPPORTED, "no launch shape for this mapping");
+        fcs_status s = ensure_gws(ctx, sh);
+        if (s != FCS_OK) return s;
+        GraphKey key;
+        std::memset(&key, 0, sizeof(key));
+        key.p = p; key.rho0 = rho0; key.T = T; key.Y = Y; key.sub = sub; key.RR = RR; key.status = status;
+        key.dtc = dtc; key.nc = nc; key.dt = dt; key.opt = ctx->opt; key.group = group; key.sorted = sorted;
+        if (!ctx->gexec || std::memcmp(&key, &ctx->gkey, sizeof(key)) != 0) {
+            if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+            ctx->gexec = nullptr;
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = enqueue_prologue();
+            WorkQueue q{ctx->bHead.p + QC_HEAD, ctx->bOrder.p, 0, ctx->bHead.p + QC_LEN};
+            if (e == cudaSuccess)
+                e = launch_integrate(sh.lc, sh.mixed, ctx->M, ko, sh.L, io, q, sh.global ? ctx->gws.p : nullptr, st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(hs, ctx->bStats.p, ST_COUNT * sizeof(long long), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(hmin, ctx->bMin.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+            cudaGraph_t gr = nullptr;
+            const cudaError_t e2 = cudaStreamEndCapture(st, &gr);
+            if (e == cudaSuccess) e = e2;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&ctx->gexec, gr, 0);
+            if (gr) cudaGraphDestroy(gr);
+            if (e != cudaSuccess) {
+                ctx->gexec = nullptr;
+                cudaGetLastError();
+                return cuda_err(ctx, e, "step graph capture");
+            }
+            std::memcpy(&ctx->gkey, &key, sizeof(key));
+        }
+        // the graph is timed as a whole (kernel_ms = the step)
+        CK(cudaEventRecord(ctx->ev0, st));
+        CK(cudaGraphLaunch(ctx->gexec, st));
+        CK(cudaEventRecord(ctx->ev1, st));
+    } else {
+        CK(enqueue_prologue());
+        int nActive = 0;
+        CK(cudaMemcpyAsync(&nActive, ctx->bHead.p + QC_LEN, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        group = ctx->opt.mapping ? ctx->opt.mapping : tuned_group(ctx, io, nActive);
+        Shape sh;
+        if (!make_shape(ctx, group, true, sh))
+            return set_err(ctx, FCS_ERR_UNSUPPORTED, "no launch shape for this mapping");
+        fcs_status s = ensure_gws(ctx, sh);
+        if (s != FCS_OK) return s;
+        WorkQueue q{ctx->bHead.p + QC_HEAD, ctx->bOrder.p, nActive};
+        CK(cudaEventRecord(ctx->ev0, st));
+        if (nActive > 0)
+            CK(launch_integrate(sh.lc, sh.mixed, ctx->M, ko, sh.L, io, q, sh.global ? ctx->gws.p : nullptr, st));
+        CK(cudaEventRecord(ctx->ev1, st));
+        hs = hsLocal;
+        CK(cudaMemcpyAsync(hs, ctx->bStats.p, ST_COUNT * sizeof(long long), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hmin, ctx->bMin.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    }
     if (!dev) {
         CK(cudaMemcpyAsync(T, io.T, nc * 8, cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(Y, io.Y, (size_t)ns * nc * 8, cudaMemcpyDeviceToHost, st));
@@ -462,6 +532,7 @@ static fcs_status integrate_impl(fcs_ctx* ctx, int64_t nc, double dt, const doub
     float ms = 0, cms = 0;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     cudaEventElapsedTime(&cms, ctx->evc0, ctx->evc1);
+    cudaGetLastError();  // an elapsed-time query that failed must not leak into the caller's next check
     if (stats) {
         stats->cells_integrated = hs[ST_CELLS];
         stats->cells_skipped = hs[ST_SKIPPED];
@@ -480,7 +551,7 @@ static fcs_status integrate_impl(fcs_ctx* ctx, int64_t nc, double dt, const doub
     }
     if (dtMin) {
         double m = 1e15;  // great
-        if (hs[ST_CELLS] > 0) std::memcpy(&m, &hmin, sizeof(m));
+        if (hs[ST_CELLS] > 0) std::memcpy(&m, hmin, sizeof(m));
         const double dref = dtc ? 0 : dt;
         *dtMin = dtc ? m : std::min(m, 2 * dref);
     }

@@ -36,6 +36,19 @@ struct DBuf {
     }
 };
 
+// What a captured step graph depends on: the arrays, sizes and options.
+struct GraphKey {
+    const void *p, *rho0, *T, *Y, *sub, *RR, *status, *dtc;
+    long long nc;
+    double dt;
+    fcs_options opt;
+    int group;
+    int sorted;
+};
+
+struct GateState;             // surrogate gate (fcs_gate.cu)
+void gate_release(fcs_ctx* ctx);
+
 struct Shape {
     LaunchCfg lc;
     SlotLayout L;
@@ -67,6 +80,12 @@ struct fcs_ctx {
     fcs::DBuf<unsigned long long> bMin;
     fcs::DBuf<char> gws;
     std::map<std::tuple<int, int, int, int>, int> tuned;  // (n, precision, solver, jac) -> group
+    fcs::GateState* gate = nullptr;                       // attached surrogate, if any
+    // CUDA-graph step (FCS_CUDA_GRAPH)
+    fcs::DBuf<int> bBin;                                  // predicted-step bin per cell
+    cudaGraphExec_t gexec = nullptr;
+    fcs::GraphKey gkey{};
+    long long* hStats = nullptr;                          // pinned: ST_COUNT counters + min sub-step bits
 };
 
 namespace fcs {

@@ -20,6 +20,73 @@ __global__ void classify_kernel(CellIO io, int ns, double Treact, int* order, in
     }
 }
 
+__device__ __forceinline__ int step_bin(double deltaT, double sub) {
+    const double steps = deltaT / fmax(sub, 1e-300);
+    int b = steps > 1 ? (int)log2(steps) : 0;
+    return b < 0 ? 0 : (b >= kQueueBins ? kQueueBins - 1 : b);
+}
+
+__global__ void classify_bin_kernel(CellIO io, int ns, double Treact, int* bin, int* counters) {
+    __shared__ int hist[kQueueBins];
+    for (int b = threadIdx.x; b < kQueueBins; b += blockDim.x) hist[b] = 0;
+    __syncthreads();
+    const long long nc = io.nCells;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < nc;
+         c += (long long)gridDim.x * blockDim.x) {
+        if (io.T[c] > Treact) {
+            const double deltaT = io.dtPerCell ? io.dtPerCell[c] : io.deltaT;
+            const int b = step_bin(deltaT, io.subDt[c]);
+            bin[c] = b;
+            atomicAdd(&hist[b], 1);
+        } else {
+            bin[c] = -1;
+            if (io.RR) for (int i = 0; i < ns; i++) io.RR[(size_t)i * nc + c] = 0;
+            if (io.status) io.status[c] = FCS_CELL_SKIPPED;
+            atomicAdd(reinterpret_cast<unsigned long long*>(&io.stats[ST_SKIPPED]), 1ull);
+        }
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < kQueueBins; b += blockDim.x)
+        if (hist[b]) atomicAdd(&counters[QC_BINS + b], hist[b]);
+}
+
+__global__ void queue_kernel(long long nc, const int* __restrict__ bin, int* counters, int* __restrict__ order) {
+    __shared__ int start[kQueueBins];
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int b = kQueueBins - 1; b >= 0; b--) {
+            start[b] = s;
+            s += counters[QC_BINS + b];
+        }
+        if (blockIdx.x == 0) counters[QC_LEN] = s;
+    }
+    __syncthreads();
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < nc;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int b = bin[c];
+        if (b >= 0) order[start[b] + atomicAdd(&counters[QC_FILL + b], 1)] = (int)c;
+    }
+}
+
+cudaError_t launch_classify_binned(const CellIO& io, int ns, double Treact, int* bin, int* counters,
+                                   cudaStream_t st) {
+    const int block = 256;
+    long long blocks = (io.nCells + block - 1) / block;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    classify_bin_kernel<<<(int)blocks, block, 0, st>>>(io, ns, Treact, bin, counters);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_queue(long long nc, const int* bin, int* counters, int* order, cudaStream_t st) {
+    const int block = 256;
+    long long blocks = (nc + block - 1) / block;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    if (blocks < 1) blocks = 1;
+    queue_kernel<<<(int)blocks, block, 0, st>>>(nc, bin, counters, order);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_integrate(const LaunchCfg& lc, bool mixed, const DevMech& M, const KOpts& o,
                              const SlotLayout& L, const CellIO& io, const WorkQueue& q, char* gws,
                              cudaStream_t st) {

@@ -681,12 +681,13 @@ integrate_kernel(const DevMech M, const KOpts o, const SlotLayout L, CellIO io, 
     long long nCells = 0, nFailed = 0;
     double dtMin = 1e300;
     int* bcast = reinterpret_cast<int*>(s.red + 40);
+    const int qn = q.nDev ? *q.nDev : q.n;
     for (;;) {
         if (g.rank == 0) bcast[0] = atomicAdd(q.head, 1);
         g.sync();
         const int idx = bcast[0];
         g.sync();
-        if (idx >= q.n) break;
+        if (idx >= qn) break;
         const long long c = q.order ? q.order[idx] : idx;
         const long long nc = io.nCells;
         const double deltaT = io.dtPerCell ? io.dtPerCell[c] : io.deltaT;

@@ -28,7 +28,14 @@ struct WorkQueue {
     int* head;                 // next queue index (atomic)
     const int* order;          // queue position -> cell, or null for identity
     int n;                     // queue length
+    const int* nDev;           // if set, the queue length is read from device memory instead
 };
+
+// Work-queue counters (int) of the binned queue: next position, length,
+// cells per bin, cells placed per bin, and a spare counter for callers.
+constexpr int kQueueBins = 32;
+enum { QC_HEAD = 0, QC_LEN = 1, QC_BINS = 2, QC_FILL = QC_BINS + kQueueBins, QC_AUX = QC_FILL + kQueueBins,
+       QC_COUNT };
 
 struct LaunchCfg {
     int group;                 // threads per cell: 32, 64, 128, 256
@@ -46,6 +53,13 @@ cudaError_t launch_eval(const LaunchCfg& lc, bool mixed, const DevMech& M, const
 cudaError_t launch_classify(const CellIO& io, int ns, double Treact, int* order, int* count,
                             cudaStream_t st);
 cudaError_t integrate_attributes(int group, bool mixed, int* maxThreads, int* regs);
+// Treact skip (as launch_classify) and, for the reacting cells, the bin of
+// their predicted step count delta_t / sub_delta_t (bin = floor(log2), 0..31);
+// bin[c] = -1 for skipped cells.
+cudaError_t launch_classify_binned(const CellIO& io, int ns, double Treact, int* bin, int* counters,
+                                   cudaStream_t st);
+// order[] = cells with bin >= 0, highest bin first; counters[QC_LEN] = their count.
+cudaError_t launch_queue(long long nc, const int* bin, int* counters, int* order, cudaStream_t st);
 
 // per-group-size instantiations (fcs_kernels_g<G>.cu)
 template<int G>

@@ -157,6 +157,7 @@ extern "C" fcs_status fcs_integrate_noalloc(fcs_ctx* ctx, int64_t nc, double dt,
     float ms = 0, cms = 0;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     cudaEventElapsedTime(&cms, ctx->evc0, ctx->evc1);
+    cudaGetLastError();  // an elapsed-time query that failed must not leak into the caller's next check
     if (stats) {
         stats->cells_integrated = hs[ST_CELLS];
         stats->cells_skipped = hs[ST_SKIPPED];

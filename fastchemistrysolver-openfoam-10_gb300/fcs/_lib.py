@@ -20,6 +20,8 @@ SOLVERS = {"OptRodas34": 0, "OptRosenbrock34": 1, "OptSeulex": 2}
 PRECISIONS = {"fp64": 0, "mixed": 1}
 JACOBIANS = {"exact": 0, "fast": 1}
 PTR_DEVICE = 1
+NO_QUEUE_SORT = 2
+CUDA_GRAPH = 4
 
 CELL_STATUS = {0: "ok", 1: "max_steps", 2: "nonfinite", 3: "dt_underflow", 4: "skipped"}
 ERRORS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "STATE", 5: "CELLS", 6: "UNSUPPORTED",
@@ -29,7 +31,13 @@ EXPORTS = ("fcs_create", "fcs_destroy", "fcs_last_error_string", "fcs_version", 
            "fcs_load_mechanism_foam", "fcs_read_chemistry_properties", "fcs_default_options",
            "fcs_set_options", "fcs_mechanism_size", "fcs_integrate", "fcs_integrate_lts",
            "fcs_integrate_noalloc", "fcs_rhs",
-           "fcs_jacobian", "fcs_rates", "fcs_bench_fp64_peak", "fcs_bench_fp32_peak", "fcs_check_exp")
+           "fcs_jacobian", "fcs_rates", "fcs_bench_fp64_peak", "fcs_bench_fp32_peak", "fcs_check_exp",
+           # include/fcs_mlp.h
+           "fcs_mlp_create", "fcs_mlp_destroy", "fcs_mlp_last_error", "fcs_mlp_get_shape", "fcs_mlp_param_count",
+           "fcs_mlp_default_train_options", "fcs_mlp_set_params", "fcs_mlp_get_params",
+           "fcs_mlp_set_normalization", "fcs_mlp_get_normalization", "fcs_mlp_forward", "fcs_mlp_gradients",
+           "fcs_mlp_train", "fcs_mlp_save", "fcs_mlp_load", "fcs_gate_default_options", "fcs_surrogate_attach",
+           "fcs_integrate_gated")
 
 
 class MechDesc(C.Structure):
@@ -57,6 +65,30 @@ class StepStats(C.Structure):
                 ("rhs_evaluations", C.c_int64), ("linear_solves", C.c_int64),
                 ("fp64_fallbacks", C.c_int64), ("kernel_ms", C.c_double), ("call_ms", C.c_double),
                 ("mapping", C.c_int32), ("reserved", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class MlpShape(C.Structure):
+    _fields_ = [("n_in", C.c_int32), ("n_out", C.c_int32), ("width", C.c_int32), ("depth", C.c_int32),
+                ("members", C.c_int32)]
+
+
+class MlpTrainOptions(C.Structure):
+    _fields_ = [("epochs", C.c_int32), ("batch", C.c_int32), ("lr", C.c_double), ("lr_final", C.c_double),
+                ("beta1", C.c_double), ("beta2", C.c_double), ("eps", C.c_double), ("seed", C.c_uint64)]
+
+
+class GateOptions(C.Structure):
+    _fields_ = [("T_rel", C.c_double), ("Y_abs", C.c_double), ("element_abs", C.c_double),
+                ("audit_fraction", C.c_double), ("seed_substep", C.c_int32), ("reserved", C.c_int32)]
+
+
+class GateStats(C.Structure):
+    _fields_ = [("cells_active", C.c_int64), ("cells_accepted", C.c_int64), ("cells_fallback", C.c_int64),
+                ("cells_audited", C.c_int64), ("audit_max_rel_T", C.c_double), ("audit_max_abs_Y", C.c_double),
+                ("surrogate_ms", C.c_double), ("integrate_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -95,6 +127,26 @@ def load(path: str = LIB) -> C.CDLL:
     L.fcs_bench_fp64_peak.argtypes = [C.c_int, C.c_double, _dp]
     L.fcs_bench_fp32_peak.argtypes = [C.c_int, C.c_double, _dp]
     L.fcs_check_exp.argtypes = [C.c_int, C.c_longlong, vp, vp, vp]
+    _fp = C.POINTER(C.c_float)
+    L.fcs_mlp_create.argtypes = [C.POINTER(vp), C.c_int, C.POINTER(MlpShape), C.c_uint64]
+    L.fcs_mlp_destroy.argtypes = [vp]
+    L.fcs_mlp_last_error.argtypes = [vp]
+    L.fcs_mlp_last_error.restype = C.c_char_p
+    L.fcs_mlp_get_shape.argtypes = [vp, C.POINTER(MlpShape)]
+    L.fcs_mlp_param_count.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.fcs_mlp_default_train_options.argtypes = [C.POINTER(MlpTrainOptions)]
+    L.fcs_mlp_set_params.argtypes = [vp, C.c_int32, vp]
+    L.fcs_mlp_get_params.argtypes = [vp, C.c_int32, vp]
+    L.fcs_mlp_set_normalization.argtypes = [vp, vp, vp, vp, vp]
+    L.fcs_mlp_get_normalization.argtypes = [vp, vp, vp, vp, vp]
+    L.fcs_mlp_forward.argtypes = [vp, C.c_int32, C.c_int64, vp, vp, C.c_int32]
+    L.fcs_mlp_gradients.argtypes = [vp, C.c_int32, C.c_int64, vp, vp, _fp, vp]
+    L.fcs_mlp_train.argtypes = [vp, C.c_int64, vp, vp, C.POINTER(MlpTrainOptions), vp]
+    L.fcs_mlp_save.argtypes = [vp, C.c_char_p]
+    L.fcs_mlp_load.argtypes = [C.POINTER(vp), C.c_int, C.c_char_p]
+    L.fcs_gate_default_options.argtypes = [C.POINTER(GateOptions)]
+    L.fcs_surrogate_attach.argtypes = [vp, vp, C.c_int32, vp, vp, C.POINTER(GateOptions)]
+    L.fcs_integrate_gated.argtypes = cell_args + [C.POINTER(GateStats)]
     _LIB = L
     return L
 
@@ -231,11 +283,12 @@ class Context:
         self.options = o
 
     def integrate_raw(self, n, dt, p, rho0, T, Y, sub, RR=None, status=None, device=False,
-                      dt_per_cell=None, check=True):
-        """Arrays are numpy (host) or torch CUDA tensors with device=True."""
+                      dt_per_cell=None, check=True, flags=0):
+        """Arrays are numpy (host) or torch CUDA tensors with device=True;
+        extra fcs_integrate flags (FCS_NO_QUEUE_SORT, FCS_CUDA_GRAPH) in `flags`."""
         stats = StepStats()
         dmin = C.c_double(0)
-        flags = PTR_DEVICE if device else 0
+        flags = (PTR_DEVICE if device else 0) | flags
         if dt_per_cell is not None:
             st = self.L.fcs_integrate_lts(self.h, n, _addr(dt_per_cell), _addr(p), _addr(rho0), _addr(T),
                                           _addr(Y), _addr(sub), _addr(RR), _addr(status), C.byref(stats),
@@ -298,3 +351,141 @@ class Context:
                                      _addr(np.ascontiguousarray(rho)), _addr(np.ascontiguousarray(Y)),
                                      _addr(RR), _addr(Q), 0))
         return RR, Q
+
+
+class Mlp:
+    """The surrogate MLP ensemble (include/fcs_mlp.h)."""
+
+    def __init__(self, n_in=None, n_out=None, width=256, depth=4, members=4, seed=0, device=0, path=None):
+        self.L = load()
+        self.h = C.c_void_p()
+        if path is not None:
+            st = self.L.fcs_mlp_load(C.byref(self.h), device, os.fsencode(path))
+            if st:
+                raise FcsError(st, f"cannot load {path}")
+        else:
+            sh = MlpShape(n_in, n_out, width, depth, members)
+            st = self.L.fcs_mlp_create(C.byref(self.h), device, C.byref(sh), seed)
+            if st:
+                raise FcsError(st, "fcs_mlp_create failed")
+        sh = MlpShape()
+        self.L.fcs_mlp_get_shape(self.h, C.byref(sh))
+        self.n_in, self.n_out, self.width, self.depth, self.members = (sh.n_in, sh.n_out, sh.width, sh.depth,
+                                                                       sh.members)
+        n = C.c_int64()
+        self.L.fcs_mlp_param_count(self.h, C.byref(n))
+        self.n_params = n.value
+
+    def close(self):
+        if self.h:
+            self.L.fcs_mlp_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st:
+            raise FcsError(st, self.L.fcs_mlp_last_error(self.h).decode())
+
+    def layer_shapes(self):
+        """[(out, in)] per layer, in parameter order."""
+        dims = [self.n_in] + [self.width] * self.depth + [self.n_out]
+        return [(dims[i + 1], dims[i]) for i in range(len(dims) - 1)]
+
+    def unflatten(self, flat):
+        out, o = [], 0
+        for (no, ni) in self.layer_shapes():
+            W = flat[o:o + no * ni].reshape(no, ni)
+            o += no * ni
+            b = flat[o:o + no]
+            o += no
+            out.append((W, b))
+        return out
+
+    def get_params(self, member):
+        p = np.zeros(self.n_params, dtype=np.float32)
+        self._check(self.L.fcs_mlp_get_params(self.h, member, _addr(p)))
+        return p
+
+    def set_params(self, member, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.n_params
+        self._check(self.L.fcs_mlp_set_params(self.h, member, _addr(p)))
+
+    def set_normalization(self, in_mean, in_std, out_mean, out_std):
+        a = [np.ascontiguousarray(v, dtype=np.float32) for v in (in_mean, in_std, out_mean, out_std)]
+        self._check(self.L.fcs_mlp_set_normalization(self.h, *[_addr(v) for v in a]))
+
+    def get_normalization(self):
+        a = [np.zeros(self.n_in, np.float32), np.zeros(self.n_in, np.float32), np.zeros(self.n_out, np.float32),
+             np.zeros(self.n_out, np.float32)]
+        self._check(self.L.fcs_mlp_get_normalization(self.h, *[_addr(v) for v in a]))
+        return a
+
+    def forward(self, member, x, device=False):
+        if device:
+            import torch
+            y = torch.empty((x.shape[0], self.n_out), dtype=torch.float32, device=x.device)
+        else:
+            x = np.ascontiguousarray(x, dtype=np.float32)
+            y = np.zeros((x.shape[0], self.n_out), dtype=np.float32)
+        self._check(self.L.fcs_mlp_forward(self.h, member, x.shape[0], _addr(x), _addr(y),
+                                           PTR_DEVICE if device else 0))
+        return y
+
+    def gradients(self, member, x, target):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        g = np.zeros(self.n_params, dtype=np.float32)
+        loss = C.c_float()
+        self._check(self.L.fcs_mlp_gradients(self.h, member, x.shape[0], _addr(x), _addr(t), C.byref(loss),
+                                             _addr(g)))
+        return loss.value, g
+
+    def train(self, x, target, epochs=20, batch=4096, lr=1e-3, lr_final=2e-5, seed=1):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        o = MlpTrainOptions()
+        self.L.fcs_mlp_default_train_options(C.byref(o))
+        o.epochs, o.batch, o.lr, o.lr_final, o.seed = epochs, batch, lr, lr_final, seed
+        hist = np.zeros((self.members, epochs), dtype=np.float32)
+        self._check(self.L.fcs_mlp_train(self.h, x.shape[0], _addr(x), _addr(t), C.byref(o), _addr(hist)))
+        return hist
+
+    def save(self, path):
+        self._check(self.L.fcs_mlp_save(self.h, os.fsencode(path)))
+
+
+def gate_options(**kw) -> GateOptions:
+    o = GateOptions()
+    load().fcs_gate_default_options(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def attach_surrogate(ctx: "Context", mlp: Optional[Mlp], composition=None, element_mass=None, **gate):
+    """Attach the ensemble to a chemistry context (None detaches)."""
+    if mlp is None:
+        ctx._check(ctx.L.fcs_surrogate_attach(ctx.h, None, 0, None, None, None))
+        return
+    comp = np.ascontiguousarray(composition, dtype=np.float64)
+    em = np.ascontiguousarray(element_mass, dtype=np.float64)
+    o = gate_options(**gate)
+    ctx._gate_keep = (mlp, comp, em, o)
+    ctx._check(ctx.L.fcs_surrogate_attach(ctx.h, mlp.h, comp.shape[1], _addr(comp), _addr(em), C.byref(o)))
+
+
+def integrate_gated_raw(ctx: "Context", n, dt, p, rho0, T, Y, sub, RR=None, status=None, device=False, check=True):
+    stats, gst = StepStats(), GateStats()
+    dmin = C.c_double(0)
+    st = ctx.L.fcs_integrate_gated(ctx.h, n, dt, _addr(p), _addr(rho0), _addr(T), _addr(Y), _addr(sub), _addr(RR),
+                                   _addr(status), C.byref(stats), C.byref(dmin), PTR_DEVICE if device else 0,
+                                   C.byref(gst))
+    if check and st not in (0, 5):
+        ctx._check(st)
+    return st, stats.as_dict(), gst.as_dict(), dmin.value

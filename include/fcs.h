@@ -89,7 +89,16 @@ enum { FCS_MAPPING_AUTO = 0, FCS_MAPPING_WARP = 32, FCS_MAPPING_BLOCK64 = 64,
 /* flags for fcs_integrate */
 enum {
     FCS_PTR_DEVICE = 1,        /* all array arguments are device pointers       */
-    FCS_NO_QUEUE_SORT = 2      /* keep natural cell order in the work queue     */
+    FCS_NO_QUEUE_SORT = 2,     /* keep natural cell order in the work queue
+                                  (default: reacting cells ordered by predicted
+                                  step count delta_t / sub_delta_t, largest first) */
+    FCS_CUDA_GRAPH = 4         /* with FCS_PTR_DEVICE: run the step as one CUDA
+                                  graph (counters, classify, queue, integrator,
+                                  statistics), captured on the first call and
+                                  replayed while the arrays, n_cells, delta_t and
+                                  options stay the same; the mapping is the
+                                  option's, else one the autotuner already chose,
+                                  else the default */
 };
 
 /*
