@@ -102,7 +102,7 @@ extern "C" const char* fcs_last_error_string(const fcs_ctx* ctx) {
 
 extern "C" fcs_status fcs_set_options(fcs_ctx* ctx, const fcs_options* o) {
     if (!ctx || !o) return FCS_ERR_INVALID;
-    if (o->solver < 0 || o->solver > 2) return set_err(ctx, FCS_ERR_INVALID, "solver must be 0..2");
+    if (o->solver < 0 || o->solver > 4) return set_err(ctx, FCS_ERR_INVALID, "solver must be 0..4");
     if (o->jacobian < 0 || o->jacobian > 1) return set_err(ctx, FCS_ERR_INVALID, "jacobian must be exact or fast");
     if (o->precision < 0 || o->precision > 1) return set_err(ctx, FCS_ERR_INVALID, "precision must be fp64 or mixed");
     if (!(o->abs_tol > 0) || !(o->rel_tol > 0)) return set_err(ctx, FCS_ERR_INVALID, "tolerances must be positive");

@@ -4,7 +4,6 @@
 // One call, all on the context's stream and without host round trips
 // between the phases:
 //   classify_kernel      T <= Treact cells: RR = 0, status skipped (as fcs_integrate)
-//   eval_kernel          f = (dY/dt, dT/dt) at the initial state (the explicit-Euler base)
 //   features_kernel      x[c] = (T, ln p, ln dt, Y_0..Y_{Ns-1})
 //   ensemble forward     members x tensor-core MLP (fcs_mlp.cu)
 //   gate_kernel          accept -> write the prediction; reject / audit -> queue bin
@@ -37,7 +36,6 @@ struct GateState {
     int ne = 0;
     DBuf<double> factor;              // [Ns][ne]: a_ei * W_e / W_i
     DBuf<float> x, y;                 // features [nc][nIn], predictions [E][nc][nOut]
-    DBuf<double> f;                   // initial-state derivatives [Ns+1][nc]
     DBuf<int> order, bin, counters, auditCell;
     DBuf<double> auditPred;           // [cap][Ns+1]: predicted Y then T
     DBuf<unsigned long long> gstats;
@@ -46,7 +44,7 @@ struct GateState {
 void gate_release(fcs_ctx* ctx) {
     if (!ctx || !ctx->gate) return;
     GateState* g = ctx->gate;
-    g->factor.release(); g->x.release(); g->y.release(); g->f.release(); g->order.release(); g->bin.release();
+    g->factor.release(); g->x.release(); g->y.release(); g->order.release(); g->bin.release();
     g->counters.release(); g->auditCell.release(); g->auditPred.release(); g->gstats.release();
     delete g;
     ctx->gate = nullptr;
@@ -81,7 +79,6 @@ struct GateArgs {
     unsigned int auditThreshold;   // of 2^32
     int seedSub, auditCap;
     const float* y;                // [E][nc][nOut]
-    const double* f;               // [Ns+1][nc] initial dY/dt, dT/dt
     const double* factor;          // [Ns][ne]
     const double* rho0;
     double* T;
@@ -116,13 +113,6 @@ __global__ void __launch_bounds__(256) gate_kernel(const GateArgs a) {
     }
     const size_t stride = (size_t)a.nc * a.nOut;
     const float* yc = a.y + (size_t)c * a.nOut;
-    // per-cell scales of the explicit-Euler corrections
-    double fmaxY = 0;
-    for (int i = lane; i < a.ns; i += 32) fmaxY = fmax(fmaxY, fabs(a.f[(size_t)i * a.nc + c]));
-    for (int o = 16; o > 0; o >>= 1) fmaxY = fmax(fmaxY, __shfl_xor_sync(0xffffffffu, fmaxY, o));
-    const double fT = a.f[(size_t)a.ns * a.nc + c];
-    const double sYc = fmax(a.dt * fmaxY, FCS_GATE_Y_SCALE_FLOOR);
-    const double sTc = fmax(a.dt * fabs(fT), FCS_GATE_T_SCALE_FLOOR);
     // T and the sub-step (every lane reads the same values)
     double mT = 0, mS = 0;
     for (int e = 0; e < a.E; e++) {
@@ -133,21 +123,20 @@ __global__ void __launch_bounds__(256) gate_kernel(const GateArgs a) {
     mS /= a.E;
     double sT = 0;
     for (int e = 0; e < a.E; e++) sT = fmax(sT, fabs((double)yc[e * stride] - mT));
-    sT *= sTc;
     // species
     double sY = 0, minY = 1e300;
     double el[kMaxElements];
     for (int k = 0; k < kMaxElements; k++) el[k] = 0;
-    bool finite = isfinite(mT) && isfinite(mS) && isfinite(fmaxY) && isfinite(fT);
+    bool finite = isfinite(mT) && isfinite(mS);
     for (int i = lane; i < a.ns; i += 32) {
         double m = 0;
         for (int e = 0; e < a.E; e++) m += yc[e * stride + 1 + i];
         m /= a.E;
         double s = 0;
         for (int e = 0; e < a.E; e++) s = fmax(s, fabs((double)yc[e * stride + 1 + i] - m));
-        const double dY = a.dt * a.f[(size_t)i * a.nc + c] + sYc * m;
+        const double dY = m;
         finite = finite && isfinite(dY);
-        sY = fmax(sY, s * sYc);
+        sY = fmax(sY, s);
         const double Yp = fmax(a.Y[(size_t)i * a.nc + c], 0.0) + dY;
         minY = fmin(minY, Yp);
         for (int k = 0; k < a.ne; k++) el[k] += a.factor[i * a.ne + k] * dY;
@@ -160,7 +149,7 @@ __global__ void __launch_bounds__(256) gate_kernel(const GateArgs a) {
     finite = __all_sync(0xffffffffu, finite);
     double elMax = 0;
     for (int k = 0; k < a.ne; k++) elMax = fmax(elMax, fabs(el[k]));
-    const double Tp = T0 + a.dt * fT + sTc * mT;
+    const double Tp = T0 + mT;
     const double subP = exp(mS);
     const bool accept = finite && isfinite(Tp) && isfinite(subP) && subP > 0 && sT <= a.Trel * T0 &&
                         sY <= a.Yabs && minY >= -a.Yabs && elMax <= a.elAbs;
@@ -182,7 +171,7 @@ __global__ void __launch_bounds__(256) gate_kernel(const GateArgs a) {
             double m = 0;
             for (int e = 0; e < a.E; e++) m += yc[e * stride + 1 + i];
             m /= a.E;
-            const double Yn = fmax(fmax(Y0, 0.0) + a.dt * a.f[ia] + sYc * m, 0.0);
+            const double Yn = fmax(fmax(Y0, 0.0) + m, 0.0);
             if (audit) {
                 if (rec) rec[i] = Yn;
             } else {
@@ -334,7 +323,6 @@ extern "C" fcs_status fcs_integrate_gated(fcs_ctx* ctx, int64_t nc, double dt, c
     CK(ctx->bMin.ensure(1));
     CK(ctx->bOrder.ensure(std::max<int64_t>(nc, 1)));
     CK(ctx->bHead.ensure(2));
-    CK(g->f.ensure((size_t)std::max<int64_t>(nc, 1) * (ns + 1)));
     CK(g->x.ensure((size_t)std::max<int64_t>(nc, 1) * nIn));
     CK(g->y.ensure((size_t)std::max<int64_t>(nc, 1) * nOut * E));
     CK(g->order.ensure(std::max<int64_t>(nc, 1)));
@@ -363,22 +351,6 @@ extern "C" fcs_status fcs_integrate_gated(fcs_ctx* ctx, int64_t nc, double dt, c
     if (nc > 0) {
         // T <= Treact: skipped exactly as by fcs_integrate (its queue is not used here)
         CK(launch_classify(io, ns, ctx->opt.T_react, ctx->bOrder.p, ctx->bHead.p + 1, st));
-        {
-            // f(y0) for every cell (the explicit-Euler base of the prediction)
-            Shape es;
-            if (!make_shape(ctx, default_group(ctx), false, es))
-                return set_err(ctx, FCS_ERR_UNSUPPORTED, "no launch shape for the derivative pass");
-            const int gpb = es.lc.block / es.lc.group;
-            es.lc.grid = (int)((nc + gpb - 1) / gpb);
-            char* gws = nullptr;
-            if (es.global) {
-                if (ctx->gws.ensure(std::max((size_t)es.lc.grid * gpb * es.L.bytes, ctx->gws.n)) != cudaSuccess)
-                    return set_err(ctx, FCS_ERR_NOMEM, "workspace allocation failed");
-                gws = ctx->gws.p;
-            }
-            CK(launch_eval(es.lc, es.mixed, ctx->M, kopts(ctx->opt), es.L, nc, io.p, io.T, nullptr, io.Y, g->f.p,
-                           nullptr, nullptr, 0, gws, st));
-        }
         const int blk = 256;
         const long long fTot = nc * nIn;
         features_kernel<<<(int)std::min<long long>((fTot + blk - 1) / blk, 152LL * 64), blk, 0, st>>>(
@@ -394,7 +366,7 @@ extern "C" fcs_status fcs_integrate_gated(fcs_ctx* ctx, int64_t nc, double dt, c
         a.Trel = g->opt.T_rel; a.Yabs = g->opt.Y_abs; a.elAbs = g->opt.element_abs;
         a.auditThreshold = (unsigned int)std::min(4294967295.0, g->opt.audit_fraction * 4294967296.0);
         a.seedSub = g->opt.seed_substep; a.auditCap = auditCap;
-        a.y = g->y.p; a.f = g->f.p; a.factor = g->factor.p; a.rho0 = io.rho0; a.T = io.T; a.Y = io.Y; a.sub = io.subDt;
+        a.y = g->y.p; a.factor = g->factor.p; a.rho0 = io.rho0; a.T = io.T; a.Y = io.Y; a.sub = io.subDt;
         a.RR = io.RR; a.status = io.status; a.bin = g->bin.p; a.counters = g->counters.p;
         a.auditCell = g->auditCell.p; a.auditPred = g->auditPred.p; a.gstats = g->gstats.p;
         a.dtMinBits = ctx->bMin.p;

@@ -313,7 +313,123 @@ __device__ __noinline__ double ros34_attempt(const Grp<G>& g, const DevMech& M, 
     return gmax(g, me, s.red);
 }
 
-// ODESolve + adaptiveSolve (OptRodas34.C:123-289, OptRosenbrock34.C:127-279),
+// OptRodas23::Rodas23Solve (OptRodas23.C:202-315), constants OptRodas23.H:113-126:
+// k2 reuses f(y0), two derivative evaluations per attempt.
+template<int G, class MT>
+__device__ __noinline__ double rodas23_attempt(const Grp<G>& g, const DevMech& M, const KOpts& o,
+                                  const Slot<MT>& s, const Slot<double>& sd, double p, double dx,
+                                  double invdx, CellCounters& cc) {
+    const int n = M.n;
+    double *y0 = s.v(0), *yTemp = s.v(1), *k1 = s.v(2), *k2 = s.v(3), *k3 = s.v(4);
+    double *dy = s.v(7), *err = s.v(8), *dydx = s.v(9), *dfdx = s.v(10), *tmp = s.v(11);
+    const double d1 = 1.0 / 2.0, d2 = 3.0 / 2.0, a31 = 2, c21 = 4, c31 = 1, c32 = -1;
+    const double c41 = 1, c42 = -1, c43 = -8.0 / 3.0;
+    const double invgamma = 1.0 / (1.0 / 2.0);
+
+    jacobian_into<G, MT>(g, M, s, sd, p, y0, dfdx, o.jacobian);
+    const double cdiag = invdx * invgamma;
+    factor_iteration<G, MT>(g, M, s, cdiag);
+    cc.jac++; cc.lu++; cc.rhs += 2; cc.solves += 4;
+
+    const double dxd1 = dx * d1, dxd2 = dx * d2;
+    for (int i = g.rank; i < n; i += G) k1[i] = fma(dxd1, dfdx[i], dfdx[i]);
+    g.sync();
+    if (!stage_solve<G, MT>(g, M, s, cdiag, k1, tmp)) return -1.0;
+    for (int i = g.rank; i < n; i += G) k2[i] = fma(dxd2, dfdx[i], dfdx[i]) + c21 * k1[i] / dx;
+    g.sync();
+    if (!stage_solve<G, MT>(g, M, s, cdiag, k2, tmp)) return -1.0;
+    for (int i = g.rank; i < n; i += G) {
+        dy[i] = a31 * k1[i];
+        yTemp[i] = y0[i] + dy[i];
+    }
+    g.sync();
+    rhs_eval<G, MT>(g, M, s, p, yTemp, dydx, 1);
+    for (int i = g.rank; i < n; i += G) k3[i] = dydx[i] + fma(c32, k2[i], c31 * k1[i]) / dx;
+    g.sync();
+    if (!stage_solve<G, MT>(g, M, s, cdiag, k3, tmp)) return -1.0;
+    for (int i = g.rank; i < n; i += G) {
+        dy[i] += k3[i];
+        yTemp[i] = y0[i] + dy[i];
+    }
+    g.sync();
+    rhs_eval<G, MT>(g, M, s, p, yTemp, dydx, 1);
+    for (int i = g.rank; i < n; i += G) err[i] = dydx[i] + fma(c43, k3[i], fma(c42, k2[i], c41 * k1[i])) / dx;
+    g.sync();
+    if (!stage_solve<G, MT>(g, M, s, cdiag, err, tmp)) return -1.0;
+    double me = 0;
+    for (int i = g.rank; i < n; i += G) {
+        const double yt = y0[i] + dy[i] + err[i];
+        yTemp[i] = yt;
+        const double tol = o.absTol + o.relTol * fmax(fabs(y0[i]), fabs(yt));
+        const double e = fabs(err[i]) / tol;
+        me = (e > me || e != e) ? e : me;
+    }
+    return gmax(g, me, s.red);
+}
+
+// OptRosenbrock23::Rosenbrock23Solve (OptRosenbrock23.C:208-298), constants
+// OptRosenbrock23.H:116-140: one derivative evaluation per attempt.
+template<int G, class MT>
+__device__ __noinline__ double ros23_attempt(const Grp<G>& g, const DevMech& M, const KOpts& o,
+                                const Slot<MT>& s, const Slot<double>& sd, double p, double dx,
+                                double invdx, CellCounters& cc) {
+    const int n = M.n;
+    double *y0 = s.v(0), *yTemp = s.v(1), *k1 = s.v(2), *k2 = s.v(3), *k3 = s.v(4);
+    double *err = s.v(8), *dydx = s.v(9), *dfdx = s.v(10), *tmp = s.v(11);
+    const double a21 = 1;
+    const double c21 = -1.0156171083877702091975600115545, c31 = 4.0759956452537699824805835358067;
+    const double c32 = 9.2076794298330791242156818474003;
+    const double b1 = 1, b2 = 6.1697947043828245592553615689730, b3 = -0.4277225654321857332623837380651;
+    const double e1 = 0.5, e2 = -2.9079558716805469821718236208017, e3 = 0.2235406989781156962736090927619;
+    const double gamma = 0.43586652150845899941601945119356, invgamma = 1.0 / gamma;
+    const double d1 = 0.43586652150845899941601945119356, d2 = 0.24291996454816804366592249683314;
+    const double d3 = 2.1851380027664058511513169485832;
+
+    jacobian_into<G, MT>(g, M, s, sd, p, y0, dfdx, o.jacobian);
+    const double cdiag = invdx * invgamma;
+    factor_iteration<G, MT>(g, M, s, cdiag);
+    cc.jac++; cc.lu++; cc.rhs += 1; cc.solves += 3;
+
+    const double dxd1 = dx * d1, dxd2 = dx * d2, dxd3 = dx * d3;
+    for (int i = g.rank; i < n; i += G) k1[i] = fma(dxd1, dfdx[i], dfdx[i]);
+    g.sync();
+    if (!stage_solve<G, MT>(g, M, s, cdiag, k1, tmp)) return -1.0;
+    for (int i = g.rank; i < n; i += G) yTemp[i] = fma(a21, k1[i], y0[i]);
+    g.sync();
+    rhs_eval<G, MT>(g, M, s, p, yTemp, dydx, 1);
+    for (int i = g.rank; i < n; i += G) k2[i] = fma(dxd2, dfdx[i], dydx[i]) + c21 * k1[i] / dx;
+    g.sync();
+    if (!stage_solve<G, MT>(g, M, s, cdiag, k2, tmp)) return -1.0;
+    for (int i = g.rank; i < n; i += G) k3[i] = fma(dxd3, dfdx[i], dydx[i]) + fma(c32, k2[i], c31 * k1[i]) / dx;
+    g.sync();
+    if (!stage_solve<G, MT>(g, M, s, cdiag, k3, tmp)) return -1.0;
+    double me = 0;
+    for (int i = g.rank; i < n; i += G) {
+        const double yt = fma(b3, k3[i], fma(b2, k2[i], fma(b1, k1[i], y0[i])));
+        yTemp[i] = yt;
+        const double e = fma(e3, k3[i], fma(e2, k2[i], e1 * k1[i]));
+        err[i] = e;
+        const double tol = o.absTol + o.relTol * fmax(fabs(y0[i]), fabs(yt));
+        const double r = fabs(e) / tol;
+        me = (r > me || r != r) ? r : me;
+    }
+    return gmax(g, me, s.red);
+}
+
+template<int G, class MT>
+__device__ __forceinline__ double attempt_of(const Grp<G>& g, const DevMech& M, const KOpts& o, const Slot<MT>& s,
+                                             const Slot<double>& sd, double p, double dx, double invdx,
+                                             CellCounters& cc) {
+    switch (o.solver) {
+        case FCS_SOLVER_ROSENBROCK34: return ros34_attempt<G, MT>(g, M, o, s, sd, p, dx, invdx, cc);
+        case FCS_SOLVER_RODAS23: return rodas23_attempt<G, MT>(g, M, o, s, sd, p, dx, invdx, cc);
+        case FCS_SOLVER_ROSENBROCK23: return ros23_attempt<G, MT>(g, M, o, s, sd, p, dx, invdx, cc);
+        default: return rodas34_attempt<G, MT>(g, M, o, s, sd, p, dx, invdx, cc);
+    }
+}
+
+// ODESolve + adaptiveSolve (OptRodas34.C:123-289, OptRosenbrock34.C:127-279,
+// OptRodas23.C:105-200, OptRosenbrock23.C:105-206),
 // with bounded reject loops.  Returns FCS_CELL_*; y0 (vector 0) holds the state.
 // One attempt in the slot's precision; in mixed precision an attempt whose
 // FP32 factorisation fails the refinement check is redone in FP64.
@@ -321,13 +437,11 @@ template<int G, class MT>
 __device__ __forceinline__ double rosenbrock_attempt(const Grp<G>& g, const DevMech& M, const KOpts& o,
                                                      const Slot<MT>& s, const Slot<double>& sd, double p,
                                                      double dx, double invdx, CellCounters& cc) {
-    double Err = o.solver == FCS_SOLVER_RODAS34 ? rodas34_attempt<G, MT>(g, M, o, s, sd, p, dx, invdx, cc)
-                                                : ros34_attempt<G, MT>(g, M, o, s, sd, p, dx, invdx, cc);
+    double Err = attempt_of<G, MT>(g, M, o, s, sd, p, dx, invdx, cc);
     if constexpr (sizeof(MT) == 4) {
         if (Err == -1.0) {
             cc.fallbacks++;
-            Err = o.solver == FCS_SOLVER_RODAS34 ? rodas34_attempt<G, double>(g, M, o, sd, sd, p, dx, invdx, cc)
-                                                 : ros34_attempt<G, double>(g, M, o, sd, sd, p, dx, invdx, cc);
+            Err = attempt_of<G, double>(g, M, o, sd, sd, p, dx, invdx, cc);
         }
     }
     return Err;

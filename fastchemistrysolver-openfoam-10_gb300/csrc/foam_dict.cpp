@@ -403,6 +403,8 @@ extern "C" fcs_status fcs_read_chemistry_properties(const char* path, fcs_option
     if (solver == "OptRodas34") o->solver = FCS_SOLVER_RODAS34;
     else if (solver == "OptRosenbrock34") o->solver = FCS_SOLVER_ROSENBROCK34;
     else if (solver == "OptSeulex") o->solver = FCS_SOLVER_SEULEX;
+    else if (solver == "OptRodas23") o->solver = FCS_SOLVER_RODAS23;
+    else if (solver == "OptRosenbrock23") o->solver = FCS_SOLVER_ROSENBROCK23;
     else return FCS_ERR_UNSUPPORTED;
     std::string jac = "exact";
     if (as_word(root.find("jacobian"), jac)) {

@@ -16,7 +16,7 @@ from .build import LIB
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
 
-SOLVERS = {"OptRodas34": 0, "OptRosenbrock34": 1, "OptSeulex": 2}
+SOLVERS = {"OptRodas34": 0, "OptRosenbrock34": 1, "OptSeulex": 2, "OptRodas23": 3, "OptRosenbrock23": 4}
 PRECISIONS = {"fp64": 0, "mixed": 1}
 JACOBIANS = {"exact": 0, "fast": 1}
 PTR_DEVICE = 1

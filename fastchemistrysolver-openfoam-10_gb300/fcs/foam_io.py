@@ -67,7 +67,7 @@ def write_chemistry_properties(path: str, solver="OptRodas34", jacobian="exact",
              "", "chemistry       on;", f"initialChemicalTimeStep {_num(initial_dt)};",
              f"jacobian {jacobian};", f"Treact {_num(treact)};",
              "balance off;", "Iter 1;", "DLBthreshold 1.1;", ""]
-    for s in ("OptRodas34", "OptRosenbrock34", "OptSeulex"):
+    for s in ("OptRodas34", "OptRosenbrock34", "OptSeulex", "OptRodas23", "OptRosenbrock23"):
         lines += [f"{s}Coeffs", "{", f"    absTol          {_num(abs_tol)};",
                   f"    relTol          {_num(rel_tol)};", "}"]
     if precision or mapping:

@@ -2,21 +2,14 @@
 
 The network, its training (forward, backward, Adam) and the gate all run in
 the library's own CUDA kernels.  This module only prepares what the network
-learns from:
-
-* cell states drawn like a workload's cells (its own generator with another
-  seed), keeping the cells that react (T > Treact);
-* their state after one CFD step and their next initial sub-step, from the
-  library's plain GPU integrator (``fcs_integrate``);
-* the derivative at the initial state (``fcs_rhs``), the explicit-Euler
-  base the gate adds the network's correction to.
+learns from: cell states drawn like a workload's cells (its own generator
+with another seed), keeping the cells that react (T > Treact), and their
+state after one CFD step and next initial sub-step from the library's plain
+GPU integrator (``fcs_integrate``).
 
 Input features (n_in = Ns + 3): T, ln p, ln dt, Y_0..Y_{Ns-1}.
-Outputs (n_out = Ns + 2):
-    r_T = (T1 - T - dt f_T) / s_T,          s_T = max(dt |f_T|, 1e-6 K)
-    r_i = (Y1_i - max(Y_i, 0) - dt f_i) / s_Y,  s_Y = max(dt max_i |f_i|, 1e-12)
-    ln sub_dt1
-exactly as the gate kernel reconstructs them.
+Outputs (n_out = Ns + 2): T1 - T, Y1_i - max(Y_i, 0), ln sub_dt1 -- exactly
+what the gate kernel adds to the cell state.
 """
 from __future__ import annotations
 
@@ -25,10 +18,6 @@ import numpy as np
 from . import _lib
 from .mechanism import ELEMENT_MASS, Mechanism
 from .workloads import Cells, Workload, cells_for
-
-T_SCALE_FLOOR = 1e-6    # FCS_GATE_T_SCALE_FLOOR
-Y_SCALE_FLOOR = 1e-12   # FCS_GATE_Y_SCALE_FLOOR
-
 
 def features(T, p, dt, Y) -> np.ndarray:
     """[n][Ns+3] float32 network inputs; Y is species-major [Ns][n]."""
@@ -41,58 +30,49 @@ def features(T, p, dt, Y) -> np.ndarray:
     return x
 
 
-def scales(f, dt):
-    """Per-cell (s_T, s_Y) from f = [Ns+1][n] derivatives at the initial state."""
-    sT = np.maximum(dt * np.abs(f[-1]), T_SCALE_FLOOR)
-    sY = np.maximum(dt * np.abs(f[:-1]).max(axis=0), Y_SCALE_FLOOR)
-    return sT, sY
-
-
-def targets(T0, Y0, f, dt, T1, Y1, sub1) -> np.ndarray:
-    sT, sY = scales(f, dt)
+def targets(T0, Y0, T1, Y1, sub1) -> np.ndarray:
     n, ns = T0.shape[0], Y0.shape[0]
     t = np.empty((n, ns + 2), dtype=np.float32)
-    t[:, 0] = (T1 - T0 - dt * f[-1]) / sT
-    t[:, 1:ns + 1] = ((Y1 - np.maximum(Y0, 0.0) - dt * f[:-1]) / sY).T
+    t[:, 0] = T1 - T0
+    t[:, 1:ns + 1] = (Y1 - np.maximum(Y0, 0.0)).T
     t[:, ns + 1] = np.log(sub1)
     return t
 
 
-def predict(mlp: _lib.Mlp, T, p, dt, Y, f):
+def predict(mlp: _lib.Mlp, T, p, dt, Y):
     """Ensemble-mean prediction (T1, Y1, sub1) in raw units, the gate's
     reconstruction restated on the host (for tests and diagnostics)."""
     x = features(T, p, dt, Y)
-    r = np.mean([mlp.forward(m, x) for m in range(mlp.members)], axis=0).astype(np.float64)
-    sT, sY = scales(f, dt)
-    T1 = T + dt * f[-1] + sT * r[:, 0]
-    Y1 = np.maximum(np.maximum(Y, 0.0) + dt * f[:-1] + sY[None, :] * r[:, 1:-1].T, 0.0)
+    # members summed in order in FP64, as the gate kernel does
+    r = np.zeros((x.shape[0], mlp.n_out))
+    for m in range(mlp.members):
+        r += mlp.forward(m, x).astype(np.float64)
+    r /= mlp.members
+    T1 = T + r[:, 0]
+    Y1 = np.maximum(np.maximum(Y, 0.0) + r[:, 1:-1].T, 0.0)
     return T1, Y1, np.exp(r[:, -1])
 
 
-def reacting_cells(w: Workload, mech: Mechanism, n: int, seed: int) -> Cells:
-    """n cells drawn like w's cells (seed offset `seed`, ...), T > Treact only."""
+def reacting_cells(w: Workload, mech: Mechanism, n: int, seed: int, per_draw: int = 1024) -> Cells:
+    """n cells drawn like w's cells, T > Treact only: `per_draw` random
+    reacting cells from each of as many seeded draws of the workload's field
+    (seed offsets seed, seed + 7919, ...) as it takes, so that the samples
+    cover many fields rather than one."""
     parts, have, k = [], 0, 0
     while have < n:
         c = cells_for(w, mech, seed_offset=seed + 7919 * k)
         keep = np.nonzero(c.T > w.treact)[0]
+        rng = np.random.default_rng(seed + 7919 * k)
+        keep = np.sort(rng.choice(keep, min(per_draw, keep.size, n - have), replace=False))
         parts.append(c.subset(keep))
         have += keep.size
         k += 1
-    T = np.concatenate([c.T for c in parts])[:n]
-    p = np.concatenate([c.p for c in parts])[:n]
-    Y = np.ascontiguousarray(np.concatenate([c.Y for c in parts], axis=1)[:, :n])
-    rho0 = np.concatenate([c.rho0 for c in parts])[:n]
-    sub = np.concatenate([c.subDt for c in parts])[:n]
+    T = np.concatenate([c.T for c in parts])
+    p = np.concatenate([c.p for c in parts])
+    Y = np.ascontiguousarray(np.concatenate([c.Y for c in parts], axis=1))
+    rho0 = np.concatenate([c.rho0 for c in parts])
+    sub = np.concatenate([c.subDt for c in parts])
     return Cells(T, p, Y, rho0, sub)
-
-
-def derivatives_device(ctx: _lib.Context, p, T, Y):
-    """fcs_rhs on torch CUDA tensors: [Ns+1][n]."""
-    import torch
-    n = T.shape[0]
-    out = torch.empty((Y.shape[0] + 1, n), dtype=torch.float64, device=T.device)
-    ctx._check(ctx.L.fcs_rhs(ctx.h, n, p.data_ptr(), T.data_ptr(), Y.data_ptr(), out.data_ptr(), _lib.PTR_DEVICE))
-    return out
 
 
 def generate(ctx: _lib.Context, cells: Cells, dt: float, chunk: int = 65536):
@@ -104,7 +84,6 @@ def generate(ctx: _lib.Context, cells: Cells, dt: float, chunk: int = 65536):
         b = min(cells.n, a + chunk)
         sub = cells.subset(np.arange(a, b))
         d = {k: torch.from_numpy(np.ascontiguousarray(getattr(sub, k))).cuda() for k in ("p", "rho0", "T", "Y", "subDt")}
-        f = derivatives_device(ctx, d["p"], d["T"], d["Y"]).cpu().numpy()
         T1, Y1, S1 = d["T"].clone(), d["Y"].clone(), d["subDt"].clone()
         st = torch.zeros(b - a, dtype=torch.int32, device="cuda")
         code, stats, _ = ctx.integrate_raw(b - a, dt, d["p"], d["rho0"], T1, Y1, S1, None, st, device=True)
@@ -112,7 +91,7 @@ def generate(ctx: _lib.Context, cells: Cells, dt: float, chunk: int = 65536):
             tot[k] += stats[k]
         ok = (st.cpu().numpy() == 0)
         x = features(sub.T, sub.p, dt, sub.Y)
-        t = targets(sub.T, sub.Y, f, dt, T1.cpu().numpy(), Y1.cpu().numpy(), S1.cpu().numpy())
+        t = targets(sub.T, sub.Y, T1.cpu().numpy(), Y1.cpu().numpy(), S1.cpu().numpy())
         xs.append(x[ok])
         ts.append(t[ok])
     return np.concatenate(xs), np.concatenate(ts), tot
@@ -123,7 +102,7 @@ def normalisation(x: np.ndarray, t: np.ndarray):
     is_ = np.maximum(x.std(axis=0), 1e-6)
     is_[2] = max(is_[2], 1.0)   # ln dt is often constant
     om = t.mean(axis=0)
-    os_ = np.maximum(t.std(axis=0), 1e-6)
+    os_ = np.maximum(t.std(axis=0), 1e-12)
     return im, is_, om, os_
 
 

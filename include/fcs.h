@@ -76,7 +76,9 @@ enum {
     FCS_RXN_SRI_FALLOFF = 5          /* (ir)reversibleArrheniusSRIFallOff          */
 };
 
-enum { FCS_SOLVER_RODAS34 = 0, FCS_SOLVER_ROSENBROCK34 = 1, FCS_SOLVER_SEULEX = 2 };
+enum { FCS_SOLVER_RODAS34 = 0, FCS_SOLVER_ROSENBROCK34 = 1, FCS_SOLVER_SEULEX = 2,
+       FCS_SOLVER_RODAS23 = 3,        /* src/ODE/OptRodas23/OptRodas23.C:202-315       */
+       FCS_SOLVER_ROSENBROCK23 = 4 }; /* src/ODE/OptRosenbrock23/OptRosenbrock23.C:208-298 */
 enum { FCS_JACOBIAN_EXACT = 0, FCS_JACOBIAN_FAST = 1 };
 /* FCS_PRECISION_MIXED: Jacobian storage and LU in FP32, one FP64-residual
  * iterative-refinement sweep per linear solve; rates, thermo, equilibrium

@@ -87,14 +87,9 @@ fcs_status fcs_mlp_load(fcs_mlp** out, int device, const char* path);
  *
  * The surrogate attached to a chemistry context has n_in = Ns + 3 inputs
  * (T, ln p, ln delta_t, Y_0 .. Y_{Ns-1}) and n_out = Ns + 2 outputs
- * (r_T, r_0 .. r_{Ns-1}, ln sub_delta_t1).  The changes over the step are
- * the explicit-Euler increment plus the network's correction in units of a
- * per-cell scale, with f = dY/dt, dT/dt at the initial state (fcs_rhs):
- *   T1   = T + dt f_T + s_T r_T,            s_T = max(dt |f_T|, FCS_GATE_T_SCALE_FLOOR)
- *   Y1_i = max(Y_i, 0) + dt f_i + s_Y r_i,  s_Y = max(dt max_i |f_i|, FCS_GATE_Y_SCALE_FLOOR)
- * so that cells that barely react are predicted to a precision that scales
- * with how much they react.  A cell's prediction (the ensemble mean) is
- * accepted when
+ * (T1 - T, Y1_0 - max(Y_0, 0) .. Y1_{Ns-1} - max(Y_{Ns-1}, 0), ln sub_delta_t1),
+ * all in raw units (the network's normalisation takes care of the scales).
+ * A cell's prediction (the ensemble mean) is accepted when
  *   - every member's T1 is within T_rel * T of the mean,
  *   - every member's Y1_i is within Y_abs of the mean, for every species,
  *   - no predicted Y1_i is below -Y_abs,
@@ -110,9 +105,6 @@ fcs_status fcs_mlp_load(fcs_mlp** out, int device, const char* path);
  * cell index) is integrated as well and keeps the plain result; the largest
  * surrogate error seen on them is reported.
  */
-#define FCS_GATE_T_SCALE_FLOOR 1e-6   /* K */
-#define FCS_GATE_Y_SCALE_FLOOR 1e-12  /* mass fraction */
-
 typedef struct fcs_gate_options {
     double T_rel;           /* default 2e-4 */
     double Y_abs;           /* default 2e-7 */

@@ -847,7 +847,100 @@ static double ros34_attempt(cellctx* c, double dx, double invdx, double* y0, dou
     return maxErr;
 }
 
-/* ODESolve + adaptiveSolve (OptRodas34.C:123-289, OptRosenbrock34.C:127-279) */
+/* OptRodas23::Rodas23Solve (OptRodas23.C:202-315), constants OptRodas23.H:113-126.
+ * k2 reuses f(y0); two derivative evaluations per attempt. */
+static double rodas23_attempt(cellctx* c, double dx, double invdx, double* y0, double* yTemp)
+{
+    const orc_mech* m = c->m; ws_t* w = c->w; const int n = m->n;
+    double *k1 = w->vec[0], *k2 = w->vec[1], *k3 = w->vec[2];
+    double *dy = w->vec[5], *err = w->vec[6], *dydx = w->vec[7], *dfdx = w->vec[8];
+    const double d1 = 1.0 / 2.0, d2 = 3.0 / 2.0, a31 = 2, c21 = 4, c31 = 1, c32 = -1;
+    const double c41 = 1, c42 = -1, c43 = -8.0 / 3.0;
+    const double invgamma = 1.0 / (1.0 / 2.0);
+    double* a = w->a;
+    jacobian(m, w, c->o, c->p, y0, dfdx, a);
+    for (int i = 0; i < n * n; i++) a[i] = -a[i];
+    for (int i = 0; i < n; i++) a[i * n + i] += invdx * invgamma;
+    lu_decompose(a, n, w->piv, w->invD);
+    w->cnt[ORC_LU]++;
+    const double dxd1 = dx * d1, dxd2 = dx * d2;
+    for (int i = 0; i < n; i++) k1[i] = fma(dxd1, dfdx[i], dfdx[i]);
+    lu_solve(a, n, w->piv, w->invD, k1);
+    for (int i = 0; i < n; i++) k2[i] = fma(dxd2, dfdx[i], dfdx[i]) + c21 * k1[i] / dx;
+    lu_solve(a, n, w->piv, w->invD, k2);
+    for (int i = 0; i < n; i++) { dy[i] = a31 * k1[i]; yTemp[i] = y0[i] + dy[i]; }
+    derivatives(m, w, c->p, yTemp, dydx, 1);
+    for (int i = 0; i < n; i++) k3[i] = dydx[i] + fma(c32, k2[i], c31 * k1[i]) / dx;
+    lu_solve(a, n, w->piv, w->invD, k3);
+    for (int i = 0; i < n; i++) { dy[i] += k3[i]; yTemp[i] = y0[i] + dy[i]; }
+    derivatives(m, w, c->p, yTemp, dydx, 1);
+    for (int i = 0; i < n; i++) err[i] = dydx[i] + fma(c43, k3[i], fma(c42, k2[i], c41 * k1[i])) / dx;
+    lu_solve(a, n, w->piv, w->invD, err);
+    w->cnt[ORC_SOLVES] += 4;
+    double maxErr = 0;
+    for (int i = 0; i < n; i++) {
+        yTemp[i] = y0[i] + dy[i] + err[i];
+        const double tol = c->o->abs_tol + c->o->rel_tol * fmax(fabs(y0[i]), fabs(yTemp[i]));
+        const double e = fabs(err[i]) / tol;
+        maxErr = maxErr > e ? maxErr : e;
+    }
+    return maxErr;
+}
+
+/* OptRosenbrock23::Rosenbrock23Solve (OptRosenbrock23.C:208-298), constants
+ * OptRosenbrock23.H:116-140.  One derivative evaluation per attempt. */
+static double ros23_attempt(cellctx* c, double dx, double invdx, double* y0, double* yTemp)
+{
+    const orc_mech* m = c->m; ws_t* w = c->w; const int n = m->n;
+    double *k1 = w->vec[0], *k2 = w->vec[1], *k3 = w->vec[2];
+    double *err = w->vec[6], *dydx = w->vec[7], *dfdx = w->vec[8];
+    const double a21 = 1;
+    const double c21 = -1.0156171083877702091975600115545, c31 = 4.0759956452537699824805835358067;
+    const double c32 = 9.2076794298330791242156818474003;
+    const double b1 = 1, b2 = 6.1697947043828245592553615689730, b3 = -0.4277225654321857332623837380651;
+    const double e1 = 0.5, e2 = -2.9079558716805469821718236208017, e3 = 0.2235406989781156962736090927619;
+    const double gamma = 0.43586652150845899941601945119356, invgamma = 1.0 / gamma;
+    const double d1 = 0.43586652150845899941601945119356, d2 = 0.24291996454816804366592249683314;
+    const double d3 = 2.1851380027664058511513169485832;
+    double* a = w->a;
+    jacobian(m, w, c->o, c->p, y0, dfdx, a);
+    for (int i = 0; i < n * n; i++) a[i] = -a[i];
+    for (int i = 0; i < n; i++) a[i * n + i] += invdx * invgamma;
+    lu_decompose(a, n, w->piv, w->invD);
+    w->cnt[ORC_LU]++;
+    const double dxd1 = dx * d1, dxd2 = dx * d2, dxd3 = dx * d3;
+    for (int i = 0; i < n; i++) k1[i] = fma(dxd1, dfdx[i], dfdx[i]);
+    lu_solve(a, n, w->piv, w->invD, k1);
+    for (int i = 0; i < n; i++) yTemp[i] = fma(a21, k1[i], y0[i]);
+    derivatives(m, w, c->p, yTemp, dydx, 1);
+    for (int i = 0; i < n; i++) k2[i] = fma(dxd2, dfdx[i], dydx[i]) + c21 * k1[i] / dx;
+    lu_solve(a, n, w->piv, w->invD, k2);
+    for (int i = 0; i < n; i++) k3[i] = fma(dxd3, dfdx[i], dydx[i]) + fma(c32, k2[i], c31 * k1[i]) / dx;
+    lu_solve(a, n, w->piv, w->invD, k3);
+    w->cnt[ORC_SOLVES] += 3;
+    double maxErr = 0;
+    for (int i = 0; i < n; i++) {
+        yTemp[i] = fma(b3, k3[i], fma(b2, k2[i], fma(b1, k1[i], y0[i])));
+        err[i] = fma(e3, k3[i], fma(e2, k2[i], e1 * k1[i]));
+        const double tol = c->o->abs_tol + c->o->rel_tol * fmax(fabs(y0[i]), fabs(yTemp[i]));
+        const double e = fabs(err[i]) / tol;
+        maxErr = maxErr > e ? maxErr : e;
+    }
+    return maxErr;
+}
+
+static double rosenbrock_attempt(cellctx* c, double dx, double invdx, double* y0, double* yTemp)
+{
+    switch (c->o->solver) {
+        case FCS_SOLVER_ROSENBROCK34: return ros34_attempt(c, dx, invdx, y0, yTemp);
+        case FCS_SOLVER_RODAS23: return rodas23_attempt(c, dx, invdx, y0, yTemp);
+        case FCS_SOLVER_ROSENBROCK23: return ros23_attempt(c, dx, invdx, y0, yTemp);
+        default: return rodas34_attempt(c, dx, invdx, y0, yTemp);
+    }
+}
+
+/* ODESolve + adaptiveSolve (OptRodas34.C:123-289, OptRosenbrock34.C:127-279,
+ * OptRodas23.C:105-200, OptRosenbrock23.C:105-206: the same controller) */
 static int rosenbrock_integrate(cellctx* c, double xEnd, double* dxTryIO, double* y0)
 {
     const double ratio = pow(MAX_SCALE / SAFE, -1.0 / ALPHA_INC);
@@ -862,8 +955,7 @@ static int rosenbrock_integrate(cellctx* c, double xEnd, double* dxTryIO, double
         const double dxTry0 = dxTry;
         if ((x + dxTry - xEnd) * (x + dxTry - 0.0) > 0) { last = 1; dxTry = xEnd - x; }
         double dx = dxTry, invdx = 1.0 / dx;
-        double Err = c->o->solver == FCS_SOLVER_RODAS34 ? rodas34_attempt(c, dx, invdx, y0, yTemp)
-                                                        : ros34_attempt(c, dx, invdx, y0, yTemp);
+        double Err = rosenbrock_attempt(c, dx, invdx, y0, yTemp);
         w->cnt[ORC_ATTEMPTS]++;
         int rejects = 0;
         while (Err > 1) {
@@ -871,8 +963,7 @@ static int rosenbrock_integrate(cellctx* c, double xEnd, double* dxTryIO, double
             const double scale = fmax(SAFE * pow(Err, -ALPHA_DEC), MIN_SCALE);
             dx *= scale;
             invdx = 1.0 / dx;
-            Err = c->o->solver == FCS_SOLVER_RODAS34 ? rodas34_attempt(c, dx, invdx, y0, yTemp)
-                                                     : ros34_attempt(c, dx, invdx, y0, yTemp);
+            Err = rosenbrock_attempt(c, dx, invdx, y0, yTemp);
             w->cnt[ORC_ATTEMPTS]++;
         }
         if (!(Err == Err)) return FCS_CELL_NONFINITE;

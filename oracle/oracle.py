@@ -20,7 +20,7 @@ PORT_SO = os.path.join(HERE, "_build", "libfcs_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libfcs_ref.so")
 REF_SRC = "/root/reference/src"
 
-SOLVERS = {"OptRodas34": 0, "OptRosenbrock34": 1, "OptSeulex": 2}
+SOLVERS = {"OptRodas34": 0, "OptRosenbrock34": 1, "OptSeulex": 2, "OptRodas23": 3, "OptRosenbrock23": 4}
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)

@@ -336,10 +336,16 @@ public:
 #include "OptRosenbrock34.C"
 #include "OptSeulex.H"
 #include "OptSeulex.C"
+#include "OptRodas23.H"
+#include "OptRodas23.C"
+#include "OptRosenbrock23.H"
+#include "OptRosenbrock23.C"
 
 template class Foam::OptRodas34<RefModel>;
 template class Foam::OptRosenbrock34<RefModel>;
 template class Foam::OptSeulex<RefModel>;
+template class Foam::OptRodas23<RefModel>;
+template class Foam::OptRosenbrock23<RefModel>;
 
 namespace {
 
@@ -370,6 +376,8 @@ std::unique_ptr<Solver> make_solver(RefHandle* h, RefConfig* cfg)
     Foam::fluidReactionThermo t{cfg};
     if (h->solver == FCS_SOLVER_RODAS34) return std::unique_ptr<Solver>(new SolverT<Foam::OptRodas34<RefModel>>(t));
     if (h->solver == FCS_SOLVER_ROSENBROCK34) return std::unique_ptr<Solver>(new SolverT<Foam::OptRosenbrock34<RefModel>>(t));
+    if (h->solver == FCS_SOLVER_RODAS23) return std::unique_ptr<Solver>(new SolverT<Foam::OptRodas23<RefModel>>(t));
+    if (h->solver == FCS_SOLVER_ROSENBROCK23) return std::unique_ptr<Solver>(new SolverT<Foam::OptRosenbrock23<RefModel>>(t));
     return std::unique_ptr<Solver>(new SolverT<Foam::OptSeulex<RefModel>>(t));
 }
 

@@ -6,7 +6,7 @@ only; needs the reference tree).  This script runs it on seeded cells of the
 synthetic workloads and stores its outputs; the tests then check the oracle
 restatement and the GPU path against these numbers on any machine.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [substring of the fixture names to regenerate]
 """
 import os
 import sys
@@ -29,6 +29,10 @@ CASES = [
     ("counterflow_53s", 8, "OptRodas34"),
     ("counterflow_53s", 4, "OptRosenbrock34"),
     ("counterflow_53s", 4, "OptSeulex"),
+    ("ignition_10s", 64, "OptRodas23"),
+    ("ignition_10s", 64, "OptRosenbrock23"),
+    ("counterflow_53s", 8, "OptRodas23"),
+    ("counterflow_53s", 4, "OptRosenbrock23"),
 ]
 
 
@@ -57,9 +61,12 @@ TIGHT = [
 ]
 
 
-def main():
+def main(only=None):
+    """Regenerate every fixture, or only those whose file name contains `only`."""
     oracle.build(ref=True)
     for wname, n in TIGHT:
+        if only and only not in f"{wname}_tight":
+            continue
         w = fcs.WORKLOADS[wname]
         mech = w.mechanism()
         flat = fcs.flatten(mech)
@@ -73,6 +80,8 @@ def main():
                             abs_tol=1e-14, rel_tol=1e-10, T=out["T"], Y=out["Y"], **inputs(flat, cells))
         print(name, os.path.getsize(name), "bytes", out["counters"])
     for wname, n, solver in CASES:
+        if only and only not in f"{wname}_{solver}":
+            continue
         w = fcs.WORKLOADS[wname]
         mech = w.mechanism()
         flat = fcs.flatten(mech)
@@ -94,4 +103,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else None)

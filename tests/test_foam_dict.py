@@ -32,3 +32,12 @@ def test_chemistry_properties_errors(tmp_path, lib_path):
         _lib.read_chemistry_properties(str(p))
     with pytest.raises(_lib.FcsError):
         _lib.read_chemistry_properties(str(tmp_path / "missing"))
+
+
+@pytest.mark.parametrize("solver,code", [("OptRodas23", 3), ("OptRosenbrock23", 4), ("OptRosenbrock34", 1)])
+def test_every_registered_solver_name(tmp_path, lib_path, solver, code):
+    """All five solvers the plugin registers (odeChemistrySolvers.C:63-74)."""
+    path = str(tmp_path / "chemistryProperties")
+    foam_io.write_chemistry_properties(path, solver=solver)
+    o, _ = _lib.read_chemistry_properties(path)
+    assert o.solver == code

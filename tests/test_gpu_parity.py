@@ -92,7 +92,9 @@ def test_fast_jacobian_matches_oracle(built):
 
 
 GOLDEN_CASES = ["ignition_10s_OptRodas34", "ignition_10s_OptRosenbrock34", "ignition_10s_OptSeulex",
-                "counterflow_53s_OptRodas34", "counterflow_53s_OptRosenbrock34", "counterflow_53s_OptSeulex"]
+                "counterflow_53s_OptRodas34", "counterflow_53s_OptRosenbrock34", "counterflow_53s_OptSeulex",
+                "ignition_10s_OptRodas23", "ignition_10s_OptRosenbrock23",
+                "counterflow_53s_OptRodas23", "counterflow_53s_OptRosenbrock23"]
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
@@ -127,7 +129,7 @@ def test_mappings_agree(built, mapping):
     np.testing.assert_allclose(out["Y"], ref["Y"], atol=1e-8)
 
 
-@pytest.mark.parametrize("solver", ["OptRodas34", "OptRosenbrock34", "OptSeulex"])
+@pytest.mark.parametrize("solver", ["OptRodas34", "OptRosenbrock34", "OptSeulex", "OptRodas23", "OptRosenbrock23"])
 def test_mixed_precision_accuracy(built, solver):
     """Mixed precision against the reference Rodas34 run at absTol 1e-14 /
     relTol 1e-10 (tests/golden/*_tight.npz).  At the workload's own tolerances

@@ -17,7 +17,9 @@ def _golden(name):
 
 
 CASES = ["ignition_10s_OptRodas34", "ignition_10s_OptRosenbrock34", "ignition_10s_OptSeulex",
-         "counterflow_53s_OptRodas34", "counterflow_53s_OptRosenbrock34", "counterflow_53s_OptSeulex"]
+         "counterflow_53s_OptRodas34", "counterflow_53s_OptRosenbrock34", "counterflow_53s_OptSeulex",
+         "ignition_10s_OptRodas23", "ignition_10s_OptRosenbrock23",
+         "counterflow_53s_OptRodas23", "counterflow_53s_OptRosenbrock23"]
 
 
 def _setup(case):
