@@ -586,8 +586,8 @@ static fcs_status eval_impl(fcs_ctx* ctx, int64_t nc, const double* p, const dou
     const int ns = ctx->M.ns, n = ctx->M.n;
     const bool dev = flags & FCS_PTR_DEVICE;
     cudaStream_t st = ctx->stream;
-    const size_t nout = (size_t)(mode == 2 ? ns : n) * nc;
-    if (mode == 2 && !rho) return set_err(ctx, FCS_ERR_INVALID, "null rho");
+    const size_t nout = (size_t)(mode == 3 ? 1 : mode == 2 ? ns : n) * nc;
+    if ((mode == 2 || mode == 3) && !rho) return set_err(ctx, FCS_ERR_INVALID, "null rho");
     const double *dp = p, *dT = T, *dY = Y, *drho = rho;
     double *dout = out, *dJ = J, *dQ = Qdot;
     if (!dev) {
@@ -597,7 +597,7 @@ static fcs_status eval_impl(fcs_ctx* ctx, int64_t nc, const double* p, const dou
         CK(cudaMemcpyAsync(ctx->bT.p, T, nc * 8, cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(ctx->bY.p, Y, (size_t)ns * nc * 8, cudaMemcpyHostToDevice, st));
         dp = ctx->bp.p; dT = ctx->bT.p; dY = ctx->bY.p; dout = ctx->bOut.p;
-        if (mode == 2) {
+        if (mode == 2 || mode == 3) {
             CK(ctx->brho.ensure(nc));
             CK(cudaMemcpyAsync(ctx->brho.p, rho, nc * 8, cudaMemcpyHostToDevice, st));
             drho = ctx->brho.p;
@@ -636,6 +636,11 @@ extern "C" fcs_status fcs_jacobian(fcs_ctx* ctx, int64_t n, const double* p, con
                                    double* J, double* dydt, int32_t flags) {
     if (!J) return set_err(ctx, FCS_ERR_INVALID, "null J");
     return eval_impl(ctx, n, p, T, nullptr, Y, dydt, J, nullptr, 1, flags);
+}
+
+extern "C" fcs_status fcs_tc(fcs_ctx* ctx, int64_t n, const double* p, const double* T, const double* rho,
+                             const double* Y, double* tc, int32_t flags) {
+    return eval_impl(ctx, n, p, T, rho, Y, tc, nullptr, nullptr, 3, flags);
 }
 
 extern "C" fcs_status fcs_rates(fcs_ctx* ctx, int64_t n, const double* p, const double* T, const double* rho,

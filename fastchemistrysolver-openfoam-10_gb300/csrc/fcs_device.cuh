@@ -87,6 +87,60 @@ __device__ __forceinline__ double gmax(const Grp<G>& g, double v, double* red) {
     }
 }
 
+// log(Tc) and 1/Tc for the whole group.  With several warps, thread 0
+// computes them and publishes them through red[44..45]; the caller's next
+// group reduction (which synchronises) makes them visible -- call
+// thermo_scalars_read after it.  A single warp computes them in every lane.
+template<int G>
+__device__ __forceinline__ void thermo_scalars_publish(const Grp<G>& g, double Tc, double* red) {
+    if constexpr (G > 32) {
+        if (g.rank == 0) { red[44] = log(Tc); red[45] = 1.0 / Tc; }
+    }
+}
+
+template<int G>
+__device__ __forceinline__ void thermo_scalars_read(const Grp<G>& g, double Tc, const double* red, double& logT,
+                                                    double& invT) {
+    if constexpr (G > 32) {
+        logT = red[44];
+        invT = red[45];
+    } else {
+        logT = log(Tc);
+        invT = 1.0 / Tc;
+    }
+}
+
+// Two maxima at once of non-negative values (or NaN, which wins), compared
+// as integers on their bit patterns: the order of non-negative doubles is the
+// order of their bits, and NaN patterns sit above +inf.  No FP64 compares.
+template<int G>
+__device__ __forceinline__ void gmax2_nonneg(const Grp<G>& g, double& a, double& b, double* red) {
+    unsigned long long x = static_cast<unsigned long long>(__double_as_longlong(a));
+    unsigned long long y = static_cast<unsigned long long>(__double_as_longlong(b));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long u = __shfl_xor_sync(0xffffffffu, x, o);
+        const unsigned long long v = __shfl_xor_sync(0xffffffffu, y, o);
+        x = u > x ? u : x;
+        y = v > y ? v : y;
+    }
+    if constexpr (G > 32) {
+        unsigned long long* r = reinterpret_cast<unsigned long long*>(red);
+        g.sync();
+        if ((g.rank & 31) == 0) { r[g.rank >> 5] = x; r[16 + (g.rank >> 5)] = y; }
+        g.sync();
+        x = r[0];
+        y = r[16];
+#pragma unroll
+        for (int w = 1; w < G / 32; w++) {
+            x = r[w] > x ? r[w] : x;
+            y = r[16 + w] > y ? r[16 + w] : y;
+        }
+    }
+    a = __longlong_as_double(static_cast<long long>(x));
+    b = __longlong_as_double(static_cast<long long>(y));
+}
+
 // ------------------------------------------------------------------------
 // slot layout (byte offsets inside one cell's workspace)
 
@@ -385,7 +439,7 @@ __device__ __noinline__ void rhs_eval(const Grp<G>& g, const DevMech& M, const S
     const int ns = M.ns;
     const double T = YT[ns];
     const double Tc = clampT(M, T);
-    const double logT = log(Tc), invT = 1.0 / Tc;
+    thermo_scalars_publish(g, Tc, s.red);
     const double RuTByP = kRu * T / p;
     double part = 0;
     for (int i = g.rank; i < ns; i += G) {
@@ -395,6 +449,8 @@ __device__ __noinline__ void rhs_eval(const Grp<G>& g, const DevMech& M, const S
         part = fma(y * __ldg(&M.invW[i]), RuTByP, part);
     }
     const double invrhoM = gsum(g, part, s.red);
+    double logT, invT;
+    thermo_scalars_read(g, Tc, s.red, logT, invT);
     const double rhoM = 1.0 / invrhoM;
     const double Tp = mode == 2 ? T : Tc;
     for (int i = g.rank; i < ns; i += G) {
@@ -456,6 +512,85 @@ __device__ __noinline__ void rhs_eval(const Grp<G>& g, const DevMech& M, const S
     gsum2(g, cpm, dtd, s.red);
     if (g.rank == 0) out[ns] = -dtd / cpm;
     g.sync();
+}
+
+// ------------------------------------------------------------------------
+// FastChemistryModel::tc (FastChemistryModel.C:589-651) over OptReaction::Tc
+// (Tc.C:3-834): c = rho Y / W (not clamped); per reaction the forward and
+// reverse molar rates summed over the products / reactants,
+// wf = n_products Kf CF and wr = n_reactants Kr CR, with Kc from the ratio of
+// Gibbs exponentials times fastPow(Pstd/(Ru T), dnu) clamped at
+// 1.49011611938476e-8; tc = sum(w) / sum(w^2) * sum(c).  Returns tc to every
+// thread.
+
+// OptReaction::fastPow (OptReaction.H:1405-1420)
+__device__ __forceinline__ double fast_pow_int(double x, int order) {
+    double xx = order < 0 ? 1 / x : x;
+    double y = 1;
+    for (int i = order; i != 0; i /= 2) {
+        if (i % 2) y *= xx;
+        xx *= xx;
+    }
+    return y;
+}
+
+template<int G, class MT>
+__device__ __noinline__ double tc_eval(const Grp<G>& g, const DevMech& M, const Slot<MT>& s, double p, double T,
+                                       double rho, const double* Y) {
+    const int ns = M.ns;
+    const double Tc = clampT(M, T);
+    const double logT = log(Tc), invT = 1.0 / Tc;
+    double sumc = 0;
+    for (int i = g.rank; i < ns; i += G) {
+        const double ci = rho * Y[i] / __ldg(&M.W[i]);
+        s.C[i] = ci;
+        sumc += ci;
+        const Nasa a = load_nasa(species_coeffs(M, i, Tc));
+        s.B[i] = fast_exp(gibbs_exponent(a, Tc, invT, logT));
+    }
+    sumc = gsum(g, sumc, s.red);
+    g.sync();
+    for (int t = g.rank; t < M.nTB; t += G) {
+        const double* e = M.eff + (size_t)t * ns;
+        double m = 0;
+        for (int j = 0; j < ns; j++) m = fma(__ldg(&e[j]), s.C[j], m);
+        s.Mtb[t] = m;
+    }
+    g.sync();
+    const double PByRT = kPstd / (kRu * Tc);
+    const double logP = M.nPlog ? log(p) : 0.0;
+    double sw = 0, sw2 = 0;
+    for (int r = g.rank; r < M.nr; r += G) {
+        const RxnInfo x = load_rx(M.rx + r);
+        double Kf;
+        if (x.kind == FCS_RXN_PLOG) {
+            double dk;
+            Kf = plog_rate(M, x.plog, p, logP, logT, invT, &dk);
+        } else if (x.tind) {
+            Kf = x.A;
+        } else {
+            Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
+        }
+        if (x.tb >= 0) Kf *= s.Mtb[x.tb];
+        double Kr = 0;
+        if (x.rev) {
+            double Kp = 1.0;
+            for (int q = 0; q < x.nl; q++) Kp = Kp / s.B[x.sl[q]];
+            for (int q = 0; q < x.nr; q++) Kp = Kp * s.B[x.sr[q]];
+            double Kc = Kp * fast_pow_int(PByRT, x.dnu);
+            Kc = Kc > 1.49011611938476e-8 ? Kc : 1.49011611938476e-8;
+            Kr = Kf / Kc;
+        }
+        double CF = s.C[x.sl[0]];
+        for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
+        double CR = s.C[x.sr[0]];
+        for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
+        const double wf = x.nr * (Kf * CF), wr = x.nl * (Kr * CR);
+        sw += wf + wr;
+        sw2 = fma(wf, wf, fma(wr, wr, sw2));
+    }
+    gsum2(g, sw, sw2, s.red);
+    return sw2 == 0 ? 1e300 : sw / sw2 * sumc;
 }
 
 // ------------------------------------------------------------------------
@@ -544,7 +679,7 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
     }
     const double T = YT[ns];
     const double Tc = clampT(M, T);
-    const double logT = log(Tc), invT = 1.0 / Tc;
+    thermo_scalars_publish(g, Tc, s.red);
     // JacobianThermo (ThermoFunctionI.H:33-371) at the clamped temperature
     const double RuTByP = (kRu * Tc) / p;
     double rs = 0, mws = 0;
@@ -554,6 +689,8 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
         mws = fma(y, invW, mws);
     }
     gsum2(g, rs, mws, s.red);
+    double logT, invT;
+    thermo_scalars_read(g, Tc, s.red, logT, invT);
     const double rhoM = 1.0 / rs, invRhoM = rs, MW = 1.0 / mws;
     double cpm = 0, dcpm = 0;
     for (int i = g.rank; i < ns; i += G) {
@@ -774,19 +911,26 @@ __device__ __noinline__ void lu_factor(const Grp<G>& g, MT* A, int n, int ld, in
             g.sync();
             break;
         }
-        const int p = choose_pivot(A, ld, k, pos, size);
+        // One thread picks the pivot row and the reciprocal of the pivot
+        // (read from that row before the interchange) and publishes both
+        // through piv[k] / invD[k]: the FP64 division and compares are issued
+        // once per column, not by every warp of the group.
+        if (g.rank == 0) {
+            const int pr = choose_pivot(A, ld, k, pos, size);
+            double akk = double(A[(size_t)pr * ld + k]);
+            if (akk == 0) akk = kPivEps;
+            invD[k] = double(MT(1.0 / akk));
+            piv[k] = pr;
+        }
+        g.sync();
+        const int p = piv[k];
+        const MT rinv = MT(invD[k]);
         if (p != k) {
-            g.sync();  // every thread has read the pivot column before rows move
             MT* rk = A + (size_t)k * ld;
             MT* rp = A + (size_t)p * ld;
             for (int j = g.rank; j < n; j += G) { const MT t = rk[j]; rk[j] = rp[j]; rp[j] = t; }
             g.sync();
         }
-        double akk = double(A[(size_t)k * ld + k]);
-        if (akk == 0) akk = kPivEps;
-        const MT rinv = MT(1.0 / akk);
-        g.sync();  // all threads read a_kk before the multipliers overwrite column k
-        if (g.rank == 0) { invD[k] = double(rinv); piv[k] = p; }
         for (int i = k + 1 + g.rank; i < n; i += G) A[(size_t)i * ld + k] *= rinv;
         g.sync();
         const MT* rk = A + (size_t)k * ld;

@@ -61,7 +61,9 @@ __device__ __noinline__ void form_iteration_matrix_scaled(const Grp<G>& g, const
                                                           double c) {
     const int ld = s.ld;
     float* LU = s.LU;
-    // pass 1: narrow -J to FP32 (the diagonal in FP64 first), row maxima
+    float* dcf = s.r32;  // FP32 copy of the column scales (the solve vector is free until the solves)
+    // pass 1: narrow c I - J to FP32 (the diagonal formed in FP64), row maxima,
+    // row scaling applied in FP32 (exact: powers of two)
     for (int i = g.rank; i < n; i += G) {
         const double* Ji = s.J64 + (size_t)i * ld;
         float* Li = LU + (size_t)i * ld;
@@ -71,21 +73,24 @@ __device__ __noinline__ void form_iteration_matrix_scaled(const Grp<G>& g, const
             Li[j] = a;
             mx = fmaxf(mx, fabsf(a));
         }
-        s.dr[i] = double(pow2_inverse(mx));
+        const float ri = pow2_inverse(mx);
+        s.dr[i] = double(ri);
+        for (int j = 0; j < n; j++) Li[j] *= ri;
     }
     g.sync();
     // pass 2: column maxima of the row-scaled matrix
     for (int j = g.rank; j < n; j += G) {
         float mx = 0.f;
-        for (int i = 0; i < n; i++) mx = fmaxf(mx, fabsf(LU[(size_t)i * ld + j] * float(s.dr[i])));
-        s.dc[j] = double(pow2_inverse(mx));
+        for (int i = 0; i < n; i++) mx = fmaxf(mx, fabsf(LU[(size_t)i * ld + j]));
+        const float cj = pow2_inverse(mx);
+        s.dc[j] = double(cj);
+        dcf[j] = cj;
     }
     g.sync();
-    // pass 3: apply both scalings (exact: powers of two)
+    // pass 3: column scaling
     for (int i = g.rank; i < n; i += G) {
         float* Li = LU + (size_t)i * ld;
-        const float ri = float(s.dr[i]);
-        for (int j = 0; j < n; j++) Li[j] = Li[j] * ri * float(s.dc[j]);
+        for (int j = 0; j < n; j++) Li[j] *= dcf[j];
     }
     g.sync();
 }
@@ -113,12 +118,13 @@ __device__ __noinline__ bool linear_solve_mixed(const Grp<G>& g, const DevMech& 
         const double d = double(s.r32[i]) * s.dc[i];
         const double x = tmp[i] + d;
         b[i] = x;
-        const double ad = fabs(d), ax = fabs(x);
-        dmax = (ad > dmax || ad != ad) ? ad : dmax;
-        xmax = (ax > xmax || ax != ax) ? ax : xmax;
+        // running maxima of |d| and |x| on the bit patterns (NaN wins)
+        const unsigned long long ad = static_cast<unsigned long long>(__double_as_longlong(fabs(d)));
+        const unsigned long long ax = static_cast<unsigned long long>(__double_as_longlong(fabs(x)));
+        if (ad > static_cast<unsigned long long>(__double_as_longlong(dmax))) dmax = fabs(d);
+        if (ax > static_cast<unsigned long long>(__double_as_longlong(xmax))) xmax = fabs(x);
     }
-    dmax = gmax(g, dmax, s.red);
-    xmax = gmax(g, xmax, s.red);
+    gmax2_nonneg(g, dmax, xmax, s.red);
     g.sync();
     return dmax <= kRefineTol * xmax && xmax < 1e300;
 }
@@ -751,7 +757,26 @@ __device__ int seulex_integrate(const Grp<G>& g, const DevMech& M, const KOpts& 
         const double dxTry0 = step.dxTry;
         step.reject = false;
         if ((x + step.dxTry - xEnd) * (x + step.dxTry - 0.0) > 0) { step.last = true; step.dxTry = xEnd - x; }
-        seulex_step<G, MT>(g, M, o, s, sd, p, sc, st, x, step, cc);
+        if constexpr (sizeof(MT) == 4) {
+            // A step whose FP32 factorisation fails the refinement check is
+            // redone in FP64 from the step's start: controller state restored,
+            // state vector from the step's saved copy (vector 1), and a fresh
+            // Jacobian (the failed attempt may have replaced the kept one).
+            const SeulexState st0 = st;
+            const SeulexStep step0 = step;
+            seulex_step<G, MT>(g, M, o, s, sd, p, sc, st, x, step, cc);
+            if (step.needFp64) {
+                cc.fallbacks++;
+                st = st0;
+                step = step0;
+                st.theta = 1e300;
+                for (int i = g.rank; i < n; i += G) s.v(0)[i] = s.v(1)[i];
+                g.sync();
+                seulex_step<G, double>(g, M, o, sd, sd, p, sc, st, x, step, cc);
+            }
+        } else {
+            seulex_step<G, MT>(g, M, o, s, sd, p, sc, st, x, step, cc);
+        }
         if (step.needFp64) return kNeedFp64;
         if (step.failed) return FCS_CELL_DT_UNDERFLOW;
         cc.accepted++;
@@ -906,9 +931,13 @@ eval_kernel(const DevMech M, const KOpts o, const SlotLayout L, long long nc, co
             const int i = idx / n, j = idx - i * n;
             Jout[(size_t)c * n * n + idx] = sd.J[(size_t)i * s.ld + j];
         }
-    } else {
+    } else if (mode == 2) {
         const double qd = rates_eval<G, MT>(g, M, s, p[c], T[c], rho[c], y, f);
         if (Qdot && g.rank == 0) Qdot[c] = qd;
+    } else {
+        const double tc = tc_eval<G, MT>(g, M, s, p[c], T[c], rho[c], y);
+        if (g.rank == 0) out[c] = tc;
+        return;
     }
     g.sync();
     const int nout = mode == 2 ? ns : n;

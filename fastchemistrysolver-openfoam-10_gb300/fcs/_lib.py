@@ -30,7 +30,7 @@ ERRORS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "STATE", 5: "CELLS", 
 EXPORTS = ("fcs_create", "fcs_destroy", "fcs_last_error_string", "fcs_version", "fcs_load_mechanism",
            "fcs_load_mechanism_foam", "fcs_read_chemistry_properties", "fcs_default_options",
            "fcs_set_options", "fcs_mechanism_size", "fcs_integrate", "fcs_integrate_lts",
-           "fcs_integrate_noalloc", "fcs_rhs",
+           "fcs_integrate_noalloc", "fcs_rhs", "fcs_tc",
            "fcs_jacobian", "fcs_rates", "fcs_bench_fp64_peak", "fcs_bench_fp32_peak", "fcs_check_exp",
            # include/fcs_mlp.h
            "fcs_mlp_create", "fcs_mlp_destroy", "fcs_mlp_last_error", "fcs_mlp_get_shape", "fcs_mlp_param_count",
@@ -124,6 +124,7 @@ def load(path: str = LIB) -> C.CDLL:
     L.fcs_rhs.argtypes = [vp, C.c_int64, vp, vp, vp, vp, C.c_int32]
     L.fcs_jacobian.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, C.c_int32]
     L.fcs_rates.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, vp, C.c_int32]
+    L.fcs_tc.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, C.c_int32]
     L.fcs_bench_fp64_peak.argtypes = [C.c_int, C.c_double, _dp]
     L.fcs_bench_fp32_peak.argtypes = [C.c_int, C.c_double, _dp]
     L.fcs_check_exp.argtypes = [C.c_int, C.c_longlong, vp, vp, vp]
@@ -342,6 +343,13 @@ class Context:
                                         _addr(np.ascontiguousarray(T)), _addr(np.ascontiguousarray(Y)),
                                         _addr(J), _addr(f), 0))
         return J, f
+
+    def tc(self, p, T, rho, Y):
+        n = T.shape[0]
+        out = np.zeros(n)
+        self._check(self.L.fcs_tc(self.h, n, _addr(np.ascontiguousarray(p)), _addr(np.ascontiguousarray(T)),
+                                  _addr(np.ascontiguousarray(rho)), _addr(np.ascontiguousarray(Y)), _addr(out), 0))
+        return out
 
     def rates(self, p, T, rho, Y):
         n = T.shape[0]

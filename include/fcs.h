@@ -299,6 +299,17 @@ fcs_status fcs_rates(fcs_ctx* ctx, int64_t n_cells, const double* p, const doubl
                      const double* rho, const double* Y, double* RR, double* Qdot,
                      int32_t flags);
 
+/*
+ * Chemical time scale per cell (FastChemistryModel::tc(),
+ * FastChemistryModel.C:589-651, over OptReaction::Tc, Tc.C:3-834):
+ * c_i = rho Y_i / W_i; for every reaction wf = n_products Kf prod(c_reactants)
+ * and wr = n_reactants Kr prod(c_products) (Kc clamped at 1.49011611938476e-8);
+ * tc = sum(wf + wr) / sum(wf^2 + wr^2) * sum_i c_i, or 1e300 when no reaction
+ * runs.  tc[n].
+ */
+fcs_status fcs_tc(fcs_ctx* ctx, int64_t n_cells, const double* p, const double* T, const double* rho,
+                  const double* Y, double* tc, int32_t flags);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1372,6 +1372,69 @@ int32_t orc_jacobian(const orc_mech* m, const orc_options* o, int64_t n_cells,
 /* FastChemistryModel::calculate (FastChemistryModel.C:715-755): c_i = rho Y_i / W_i
  * (no clamp), RR_i = dNdtByV_i W_i; Qdot = -sum Hf_i RR_i (FastChemistryModel.C:656-685)
  * with Hf the janaf enthalpy at 298.15 K. */
+/* OptReaction::fastPow (OptReaction.H:1405-1420) */
+static double fast_pow(double x, int order)
+{
+    double xx = order < 0 ? 1 / x : x;
+    double y = 1;
+    for (int i = order; i != 0; i /= 2) {
+        if (i % 2) y *= xx;
+        xx *= xx;
+    }
+    return y;
+}
+
+/* FastChemistryModel::tc (FastChemistryModel.C:589-651) over OptReaction::Tc
+ * (Tc.C:3-834): per reaction wf = n_products Kf CF, wr = n_reactants Kr CR,
+ * tc = sum(w) / sum(w^2) * sum(c), c = rho Y / W (Y not clamped). */
+int32_t orc_tc(const orc_mech* m, int64_t n_cells, const double* p, const double* T, const double* rho,
+               const double* Y, double* tc)
+{
+    ws_t* w = ws_create(m);
+    const int ns = m->ns;
+    for (int64_t c = 0; c < n_cells; c++) {
+        double sumc = 0;
+        for (int i = 0; i < ns; i++) {
+            w->C[i] = rho[c] * Y[(size_t)i * n_cells + c] / m->W[i];
+            sumc += w->C[i];
+        }
+        double Tc = T[c] < m->TlowMin ? m->TlowMin : T[c];
+        Tc = Tc > m->ThighMax ? m->ThighMax : Tc;
+        const double logT = log(Tc), invT = 1.0 / Tc;
+        for (int i = 0; i < ns; i++) w->B[i] = exp(gibbs_exponent(coeffs(m, i, Tc), Tc, invT, logT));
+        const double PByRT = PSTD / (RU * Tc);
+        arrhenius_rates(m, w, logT, invT, 0);
+        third_body(m, w);
+        for (int i = 0; i < m->nr; i++)
+            if (m->kind[i] == FCS_RXN_THIRD_BODY) w->Kf[i] *= w->M[m->tbRow[i]];
+        if (m->nPlog) plog_rates(m, w, p[c], logT, invT, 0);
+        double sumW = 0, sumWR = 0;
+        for (int i = 0; i < m->nr; i++) {
+            const double Kf = (m->kind[i] == FCS_RXN_PLOG) ? w->Kplog[m->plogIdx[i]] : w->Kf[i];
+            const int* L = &m->lSp[m->lOff[i]];
+            const int* R = &m->rSp[m->rOff[i]];
+            const int nl = m->lOff[i + 1] - m->lOff[i], nr = m->rOff[i + 1] - m->rOff[i];
+            double Kr = 0, Kp = 1.0;
+            if (m->rev[i]) {
+                for (int q = 0; q < nl; q++) Kp = Kp / w->B[L[q]];
+                for (int q = 0; q < nr; q++) Kp = Kp * w->B[R[q]];
+                double Kc = Kp * fast_pow(PByRT, nr - nl);
+                Kc = Kc > KC_CLAMP_G ? Kc : KC_CLAMP_G;
+                Kr = Kf / Kc;
+            }
+            const double wf = nr * (Kf * prod_sp(L, nl, w->C));
+            const double wr = nl * (Kr * prod_sp(R, nr, w->C));
+            sumW += wf;
+            sumWR += wf * wf;
+            sumW += wr;
+            sumWR += wr * wr;
+        }
+        tc[c] = sumWR == 0 ? 1e300 : sumW / sumWR * sumc;
+    }
+    ws_destroy(w);
+    return FCS_OK;
+}
+
 int32_t orc_rates(const orc_mech* m, int64_t n_cells, const double* p, const double* T, const double* rho,
                   const double* Y, double* RR, double* Qdot)
 {

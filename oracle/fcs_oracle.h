@@ -61,6 +61,9 @@ int32_t orc_jacobian(const orc_mech* m, const orc_options* o, int64_t n_cells,
 /* calculate(): RR [Ns*n] and Qdot [n] from (p, T, rho, Y) */
 int32_t orc_rates(const orc_mech* m, int64_t n_cells, const double* p, const double* T, const double* rho,
                   const double* Y, double* RR, double* Qdot);
+/* FastChemistryModel::tc (chemical time scale) per cell from (p, T, rho, Y) */
+int32_t orc_tc(const orc_mech* m, int64_t n_cells, const double* p, const double* T, const double* rho,
+               const double* Y, double* tc);
 /* Dense LU with the reference's 4-row-panel pivoting on one n x n row-major
  * matrix; solves nrhs right-hand sides in place (b is [nrhs][n]). */
 int32_t orc_lu_solve(int32_t n, double* a, int32_t nrhs, double* b, int32_t* piv,

@@ -103,6 +103,7 @@ class Port:
         L.orc_lu_solve.argtypes = [C.c_int32, _dp, C.c_int32, _dp, _ip, _dp]
         L.orc_mech_order.argtypes = [C.c_void_p, _ip]
         L.orc_rates.argtypes = [C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.orc_tc.argtypes = [C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp, _dp]
         self.ns = flat.n_species
         self.nr = flat.n_reactions
         self.desc = make_desc(flat)
@@ -181,6 +182,13 @@ class Port:
                            _ptr(np.ascontiguousarray(rho)), _ptr(np.ascontiguousarray(Y)), _ptr(RR), _ptr(Q))
         return RR, Q
 
+    def tc(self, p, T, rho, Y):
+        n = T.shape[0]
+        out = np.zeros(n)
+        self.lib.orc_tc(self.h, n, _ptr(np.ascontiguousarray(p)), _ptr(np.ascontiguousarray(T)),
+                        _ptr(np.ascontiguousarray(rho)), _ptr(np.ascontiguousarray(Y)), _ptr(out))
+        return out
+
     def lu_solve(self, a, b):
         a = np.ascontiguousarray(a, dtype=np.float64).copy()
         b = np.ascontiguousarray(b, dtype=np.float64).copy()
@@ -208,6 +216,7 @@ class Reference:
         L.ref_rhs.argtypes = [C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp]
         L.ref_jacobian.argtypes = [C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp, _dp]
         L.ref_lu_solve.argtypes = [C.c_int, _dp, C.c_int, _dp]
+        L.ref_tc.argtypes = [C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp, _dp]
         self.ns = flat.n_species
         self.desc = make_desc(flat)
         self.h = L.ref_create(C.byref(self.desc), SOLVERS[solver], 0 if jacobian == "exact" else 1,
@@ -251,6 +260,13 @@ class Reference:
         self.lib.ref_jacobian(self.h, n, _ptr(np.ascontiguousarray(p)), _ptr(np.ascontiguousarray(T)),
                               _ptr(np.ascontiguousarray(Y)), _ptr(J), _ptr(f))
         return J, f
+
+    def tc(self, p, T, rho, Y):
+        n = T.shape[0]
+        out = np.zeros(n)
+        self.lib.ref_tc(self.h, n, _ptr(np.ascontiguousarray(p)), _ptr(np.ascontiguousarray(T)),
+                        _ptr(np.ascontiguousarray(rho)), _ptr(np.ascontiguousarray(Y)), _ptr(out))
+        return out
 
     def lu_solve(self, a, b):
         a = np.ascontiguousarray(a, dtype=np.float64).copy()

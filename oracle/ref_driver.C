@@ -16,6 +16,7 @@
 #include "OptReaction.H"
 #include "Jacobian.C"
 #include "ReactionRate.C"
+#include "Tc.C"
 
 #include "chemistrySolver.H"
 #include "LUsolver.H"
@@ -532,6 +533,30 @@ int ref_jacobian(void* handle, int64_t n, const double* p, const double* T, cons
         y[ns] = T[c];
         m.jacobian(0, y.data(), int(c), f.data(), &J[(size_t)c * nn * nn]);
         for (int i = 0; i < nn; i++) dydt[(size_t)i * n + c] = f[i];
+    }
+    return 0;
+}
+
+// FastChemistryModel::tc (FastChemistryModel.C:589-651) over OptReaction::Tc
+// (Tc.C:3-834): c = rho Y / W, tc = sumW / sumWRateByCTot * sum(c)
+int ref_tc(void* handle, int64_t n, const double* p, const double* T, const double* rho, const double* Y,
+           double* tc)
+{
+    RefHandle* h = static_cast<RefHandle*>(handle);
+    RefConfig cfg{&h->desc, h->jacobian, h->absTol, h->relTol, h->maxSteps, p};
+    Foam::fluidReactionThermo t{&cfg};
+    RefModel m(t);
+    const int ns = h->desc.n_species;
+    std::vector<double> c(ns);
+    for (int64_t k = 0; k < n; k++) {
+        double sumc = 0;
+        for (int i = 0; i < ns; i++) {
+            c[i] = rho[k] * Y[(size_t)i * n + k] / h->desc.W[i];
+            sumc += c[i];
+        }
+        double sumW = 0, sumWR = 0;
+        m.reaction.Tc(int(k), p[k], T[k], c.data(), sumW, sumWR);
+        tc[k] = sumWR == 0 ? Foam::vGreat : sumW / sumWR * sumc;
     }
     return 0;
 }

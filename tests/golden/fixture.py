@@ -32,3 +32,16 @@ def check_generator(g, wname):
     cells = fcs.cells_for(w, mech).subset(g["cell_index"])
     np.testing.assert_allclose(cells.T, g["in_T"], rtol=1e-12)
     np.testing.assert_allclose(cells.Y, g["in_Y"], rtol=1e-9, atol=1e-15)
+
+
+class _Prefixed:
+    def __init__(self, g, prefix):
+        self.g, self.prefix = g, prefix
+
+    def __getitem__(self, k):
+        return self.g[self.prefix + k]
+
+
+def load_prefixed(g, prefix):
+    """load() for a fixture that stores several cases under '<prefix>' keys."""
+    return load(_Prefixed(g, prefix))

@@ -61,9 +61,36 @@ TIGHT = [
 ]
 
 
+TC = [
+    # (workload, cells): FastChemistryModel::tc() of the reference on the workload's cells
+    ("ignition_10s", 64),
+    ("counterflow_53s", 64),
+    ("uneven_111s", 64),
+]
+
+
+def make_tc():
+    out = {}
+    for wname, n in TC:
+        w = fcs.WORKLOADS[wname]
+        mech = w.mechanism()
+        flat = fcs.flatten(mech)
+        idx = cell_index(w, n)
+        cells = fcs.cells_for(w, mech).subset(idx)
+        tc = oracle.Reference(flat).tc(cells.p, cells.T, cells.rho0, cells.Y)
+        for k, v in inputs(flat, cells).items():
+            out[f"{wname}__{k}"] = v
+        out[f"{wname}__tc"] = tc
+    name = os.path.join(HERE, "tc.npz")
+    np.savez_compressed(name, **out)
+    print(name, os.path.getsize(name), "bytes")
+
+
 def main(only=None):
     """Regenerate every fixture, or only those whose file name contains `only`."""
     oracle.build(ref=True)
+    if not only or only in "tc":
+        make_tc()
     for wname, n in TIGHT:
         if only and only not in f"{wname}_tight":
             continue

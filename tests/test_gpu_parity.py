@@ -297,3 +297,14 @@ def test_queue_order_and_graph_replay_do_not_change_results(built):
         assert m == m0
         for k in ("cells_integrated", "cells_skipped", "attempts", "accepted", "jacobians"):
             assert s[k] == s0[k], k
+
+
+@pytest.mark.parametrize("wname", ["ignition_10s", "counterflow_53s", "uneven_111s"])
+def test_tc_matches_reference_golden(built, wname):
+    """fcs_tc against FastChemistryModel::tc() of the reference
+    (tests/golden/tc.npz); differences are summation order and exp rounding."""
+    g = np.load(os.path.join(GOLDEN, "tc.npz"))
+    flat, c = fixture.load_prefixed(g, wname + "__")
+    ctx = _ctx(flat)
+    tc = ctx.tc(c.p, c.T, c.rho0, c.Y)
+    np.testing.assert_allclose(tc, g[wname + "__tc"], rtol=1e-12)

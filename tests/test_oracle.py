@@ -118,3 +118,13 @@ def test_port_against_compiled_reference_directly(port_built):
     assert (r0["status"] == r1["status"]).all()
     np.testing.assert_allclose(r1["T"], r0["T"], rtol=1e-8)
     np.testing.assert_allclose(r1["Y"], r0["Y"], atol=1e-9)
+
+
+@pytest.mark.parametrize("wname", ["ignition_10s", "counterflow_53s", "uneven_111s"])
+def test_port_tc_matches_reference_golden(wname, port_built):
+    """FastChemistryModel::tc() of the reference (tests/golden/tc.npz)."""
+    import oracle
+    g = _golden("tc")
+    flat, cells = fixture.load_prefixed(g, wname + "__")
+    tc = oracle.Port(flat).tc(cells.p, cells.T, cells.rho0, cells.Y)
+    np.testing.assert_allclose(tc, g[wname + "__tc"], rtol=1e-13)
