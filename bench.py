@@ -63,8 +63,9 @@ def parse():
     ap.add_argument("--cells", type=int, default=0, help="0: the workload's full cell count")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--method", default="both", choices=["plain", "gated", "both"],
-                    help="plain GPU method, the surrogate-gated method, or both on the same cells")
+    ap.add_argument("--method", default="both", choices=["plain", "gated", "both", "mlp"],
+                    help="plain GPU method, the surrogate-gated method, or both on the same cells; "
+                         "mlp: only the ensemble forward on the tensor cores (untrained weights)")
     ap.add_argument("--train-samples", type=int, default=65536,
                     help="cells integrated by the plain method to train the surrogate (before timing)")
     ap.add_argument("--accuracy-cells", type=int, default=256,
@@ -255,10 +256,45 @@ def args_solver(o):
     return {v: k for k, v in _lib.SOLVERS.items()}[o.solver]
 
 
+def mlp_bench(args):
+    """The surrogate ensemble's forward over the field on the tensor cores
+    (tcgen05 GEMMs): the profiling case of the MLP kernels."""
+    import torch
+    import fcs
+    from fcs import _lib, surrogate
+    w = fcs.WORKLOADS[args.workload]
+    mech = w.mechanism()
+    cells = fcs.cells_for(w, mech, n=args.cells or None)
+    ns, n = mech.n_species, cells.n
+    mlp = _lib.Mlp(ns + 3, ns + 2, width=256, depth=4, members=4, seed=1)
+    x = torch.from_numpy(surrogate.features(cells.T, cells.p, w.dt, cells.Y)).cuda()
+    mlp.set_normalization(x.mean(0).cpu().numpy(), x.std(0).cpu().numpy().clip(1e-6), np.zeros(ns + 2),
+                          np.ones(ns + 2))
+    for _ in range(args.warmup):
+        for m in range(mlp.members):
+            mlp.forward(m, x, device=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        for m in range(mlp.members):
+            mlp.forward(m, x, device=True)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    dims = [ns + 3] + [256] * 4 + [ns + 2]
+    flop = 2.0 * n * 4 * sum(dims[i] * dims[i + 1] for i in range(len(dims) - 1))
+    print(json.dumps({"mlp_forward": {"workload": w.name, "cells": n, "members": 4, "ms_per_ensemble": ms,
+                                      "tflops": flop / (ms * 1e-3) / 1e12, "steps": args.steps,
+                                      "warmup": args.warmup}}), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.method == "mlp":
+        return mlp_bench(args)
     ws, rank, local = dist_info()
     import torch
     if ws > 1:
