@@ -474,39 +474,25 @@ __device__ __noinline__ void rhs_eval(const Grp<G>& g, const DevMech& M, const S
     g.sync();
     const PFactor pf = pressure_factors(Tc);
     const double logP = M.nPlog ? log(p) : 0.0;
-    // Two reactions per thread and pass (r and r + G), written as one
-    // straight-line body so that their exp chains interleave: the FP64 unit
-    // of a sub-partition completes a warp instruction only every few dozen
-    // cycles, and a single dependent chain per warp leaves it idle.
-    for (int r0 = g.rank; r0 < M.nr; r0 += 2 * G) {
-        const int r1 = r0 + G < M.nr ? r0 + G : r0;
-        const RxnInfo x0 = load_rx(M.rx + r0);
-        const RxnInfo x1 = load_rx(M.rx + r1);
-        double e0 = 0, e1 = 0;
-        if (x0.kind != FCS_RXN_PLOG && !x0.tind) e0 = fast_exp(fma(x0.beta, logT, -(x0.Ta * invT)));
-        if (x1.kind != FCS_RXN_PLOG && !x1.tind) e1 = fast_exp(fma(x1.beta, logT, -(x1.Ta * invT)));
-        double Kf0 = x0.tind ? x0.A : x0.A * e0;
-        double Kf1 = x1.tind ? x1.A : x1.A * e1;
-        if (x0.kind == FCS_RXN_PLOG) {
+    for (int r = g.rank; r < M.nr; r += G) {
+        const RxnInfo x = load_rx(M.rx + r);
+        double Kf;
+        if (x.kind == FCS_RXN_PLOG) {
             double dk;
-            Kf0 = plog_rate(M, x0.plog, p, logP, logT, invT, &dk);
+            Kf = plog_rate(M, x.plog, p, logP, logT, invT, &dk);
+        } else if (x.tind) {
+            Kf = x.A;
+        } else {
+            Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
         }
-        if (x1.kind == FCS_RXN_PLOG) {
-            double dk;
-            Kf1 = plog_rate(M, x1.plog, p, logP, logT, invT, &dk);
-        }
-        if (x0.tb >= 0) Kf0 *= s.Mtb[x0.tb];
-        if (x1.tb >= 0) Kf1 *= s.Mtb[x1.tb];
-        const double Kr0 = x0.rev ? Kf0 * inv_equilibrium_kc(x0, s.B, s.Binv, pf) : 0.0;
-        const double Kr1 = x1.rev ? Kf1 * inv_equilibrium_kc(x1, s.B, s.Binv, pf) : 0.0;
-        double CF0 = s.C[x0.sl[0]], CF1 = s.C[x1.sl[0]];
-        for (int q = 1; q < x0.nl; q++) CF0 *= s.C[x0.sl[q]];
-        for (int q = 1; q < x1.nl; q++) CF1 *= s.C[x1.sl[q]];
-        double CR0 = s.C[x0.sr[0]], CR1 = s.C[x1.sr[0]];
-        for (int q = 1; q < x0.nr; q++) CR0 *= s.C[x0.sr[q]];
-        for (int q = 1; q < x1.nr; q++) CR1 *= s.C[x1.sr[q]];
-        s.q[r0] = Kf0 * CF0 - Kr0 * CR0;
-        if (r1 != r0) s.q[r1] = Kf1 * CF1 - Kr1 * CR1;
+        if (x.tb >= 0) Kf *= s.Mtb[x.tb];
+        double Kr = 0;
+        if (x.rev) Kr = Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
+        double CF = s.C[x.sl[0]];
+        for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
+        double CR = s.C[x.sr[0]];
+        for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
+        s.q[r] = Kf * CF - Kr * CR;
     }
     g.sync();
     double cpm = 0, dtd = 0;
