@@ -73,6 +73,18 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(value: float, device=None) -> float:
+    """The largest of every rank's value (the whole-job step time is the
+    slowest replica's); the value itself when not distributed."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return value
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_info():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -354,12 +366,7 @@ def main():
             times.append(r[0])
             out.append(r)
         torch.cuda.synchronize()
-        t = statistics.mean(times)
-        if ws > 1:
-            tt = torch.tensor([t], device=dev)
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            t = float(tt.item())
-        return t, out
+        return max_over_ranks(statistics.mean(times), dev), out
 
     # the first call autotunes the cell-to-thread mapping (outside the graph)
     step_plain(graph=False)
@@ -386,11 +393,7 @@ def main():
                                               hS.numpy(), hRR.numpy(), hst.numpy())
         if i >= 1:
             e2e_ms.append(stats["call_ms"])
-    t_e2e = statistics.mean(e2e_ms)
-    if ws > 1:
-        tt = torch.tensor([t_e2e], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(tt.item())
+    t_e2e = max_over_ranks(statistics.mean(e2e_ms), dev)
     h2d = 8 * n * (4 + ns)
     d2h = 8 * n * (2 + 2 * ns) + 4 * n
     # the surrogate-gated method on the same cells
