@@ -265,6 +265,10 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
     M.nTbInc = nTbInc; M.tbInc = ctx->dTbInc.p;
     ctx->loaded = true;
     ctx->tuned.clear();
+    if (ctx->gexec) {  // a captured step holds the old mechanism's scalars
+        cudaGraphExecDestroy(ctx->gexec);
+        ctx->gexec = nullptr;
+    }
     return FCS_OK;
 }
 
@@ -474,6 +478,10 @@ static fcs_status integrate_impl(fcs_ctx* ctx, int64_t nc, double dt, const doub
         std::memset(&key, 0, sizeof(key));
         key.p = p; key.rho0 = rho0; key.T = T; key.Y = Y; key.sub = sub; key.RR = RR; key.status = status;
         key.dtc = dtc; key.nc = nc; key.dt = dt; key.opt = ctx->opt; key.group = group; key.sorted = sorted;
+        key.internal[0] = ctx->bStats.p; key.internal[1] = ctx->bMin.p; key.internal[2] = ctx->bHead.p;
+        key.internal[3] = ctx->bOrder.p; key.internal[4] = ctx->bBin.p; key.internal[5] = ctx->gws.p;
+        key.internal[6] = ctx->hStats;
+        key.mech = ctx->M.rx;
         if (!ctx->gexec || std::memcmp(&key, &ctx->gkey, sizeof(key)) != 0) {
             if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
             ctx->gexec = nullptr;

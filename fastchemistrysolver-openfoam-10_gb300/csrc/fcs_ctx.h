@@ -39,6 +39,8 @@ struct DBuf {
 // What a captured step graph depends on: the arrays, sizes and options.
 struct GraphKey {
     const void *p, *rho0, *T, *Y, *sub, *RR, *status, *dtc;
+    const void* internal[8];  // the context's buffers the graph uses (they move when they grow)
+    const void* mech;         // the mechanism's device arrays (reloading replaces them)
     long long nc;
     double dt;
     fcs_options opt;

@@ -308,3 +308,34 @@ def test_tc_matches_reference_golden(built, wname):
     ctx = _ctx(flat)
     tc = ctx.tc(c.p, c.T, c.rho0, c.Y)
     np.testing.assert_allclose(tc, g[wname + "__tc"], rtol=1e-12)
+
+
+def test_graph_step_recaptures_when_buffers_or_mechanism_change(built):
+    """A replayed step graph never uses a buffer that a larger call has
+    replaced, nor a mechanism that has been reloaded."""
+    import torch
+    from fcs._lib import CUDA_GRAPH
+    w, mech, flat, c = _setup("ignition_10s", 64)
+    ctx = _ctx(flat, abs_tol=w.abs_tol, rel_tol=w.rel_tol, mapping=64)
+    d = {k: torch.from_numpy(np.ascontiguousarray(getattr(c, k))).cuda() for k in ("p", "rho0", "T", "Y", "subDt")}
+    init = {k: v.clone() for k, v in d.items()}
+
+    def step():
+        for k in d:
+            d[k].copy_(init[k])
+        code, stats, _ = ctx.integrate_raw(c.n, w.dt, d["p"], d["rho0"], d["T"], d["Y"], d["subDt"], device=True,
+                                           flags=CUDA_GRAPH)
+        assert code == 0
+        return d["T"].clone(), stats["attempts"]
+
+    T1, a1 = step()
+    # a larger ordinary call grows (and so moves) the context's internal buffers
+    big = fcs.cells_for(w, mech, n=1024)
+    ctx.integrate(big, w.dt)
+    T2, a2 = step()
+    assert torch.equal(T1, T2) and a1 == a2
+    # reloading the mechanism invalidates the captured step
+    ctx.load_mechanism(flat)
+    ctx.set_options(abs_tol=w.abs_tol, rel_tol=w.rel_tol, mapping=64)
+    T3, a3 = step()
+    assert torch.equal(T1, T3) and a1 == a3
