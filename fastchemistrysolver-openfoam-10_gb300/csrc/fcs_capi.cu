@@ -87,6 +87,7 @@ extern "C" fcs_status fcs_destroy(fcs_ctx* ctx) {
     ctx->bStats.release(); ctx->bMin.release(); ctx->gws.release(); ctx->bBin.release();
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     if (ctx->hStats) cudaFreeHost(ctx->hStats);
+    if (ctx->evAsync) cudaEventDestroy(ctx->evAsync);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->evc0) cudaEventDestroy(ctx->evc0);
@@ -322,7 +323,7 @@ bool fcs::make_shape(fcs_ctx* ctx, int group, bool integrate, Shape& sh) {
     return true;
 }
 
-static fcs_status ensure_gws(fcs_ctx* ctx, const Shape& sh) {
+fcs_status fcs::ensure_gws(fcs_ctx* ctx, const Shape& sh) {
     if (!sh.global) return FCS_OK;
     const size_t groups = (size_t)sh.lc.grid * (sh.lc.block / sh.lc.group);
     if (ctx->gws.ensure(groups * (size_t)sh.L.bytes) != cudaSuccess)
@@ -334,6 +335,13 @@ int fcs::default_group(fcs_ctx* ctx) {
     const int n = ctx->M.n;
     if (n <= 128) return 64;
     return 128;
+}
+
+int fcs::cached_group(fcs_ctx* ctx) {
+    if (ctx->opt.mapping) return ctx->opt.mapping;
+    const auto it = ctx->tuned.find(
+        std::make_tuple(ctx->M.n, (int)ctx->opt.precision, (int)ctx->opt.solver, (int)ctx->opt.jacobian));
+    return it != ctx->tuned.end() ? it->second : default_group(ctx);
 }
 
 // Autotuner for FCS_MAPPING_AUTO: times every candidate cell-to-thread

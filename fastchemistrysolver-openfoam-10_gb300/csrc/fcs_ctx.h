@@ -88,6 +88,11 @@ struct fcs_ctx {
     cudaGraphExec_t gexec = nullptr;
     fcs::GraphKey gkey{};
     long long* hStats = nullptr;                          // pinned: ST_COUNT counters + min sub-step bits
+    // asynchronous step (fcs_integrate_async / fcs_sync)
+    cudaEvent_t evAsync = nullptr;
+    bool asyncPending = false;
+    double asyncDt = 0;
+    int asyncGroup = 0;
 };
 
 namespace fcs {
@@ -98,6 +103,10 @@ KOpts kopts(const fcs_options& o);
 // Launch shape for a group size; false when impossible.
 bool make_shape(fcs_ctx* ctx, int group, bool integrate, Shape& sh);
 int default_group(fcs_ctx* ctx);
+// The option's mapping, else one the autotuner cached for this key, else the default.
+int cached_group(fcs_ctx* ctx);
+// Global-memory workspace for shapes whose slot exceeds shared memory.
+fcs_status ensure_gws(fcs_ctx* ctx, const Shape& sh);
 
 }  // namespace fcs
 

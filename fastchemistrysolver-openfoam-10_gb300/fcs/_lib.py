@@ -30,7 +30,7 @@ ERRORS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "STATE", 5: "CELLS", 
 EXPORTS = ("fcs_create", "fcs_destroy", "fcs_last_error_string", "fcs_version", "fcs_load_mechanism",
            "fcs_load_mechanism_foam", "fcs_read_chemistry_properties", "fcs_default_options",
            "fcs_set_options", "fcs_mechanism_size", "fcs_integrate", "fcs_integrate_lts",
-           "fcs_integrate_noalloc", "fcs_rhs", "fcs_tc",
+           "fcs_integrate_noalloc", "fcs_integrate_async", "fcs_sync", "fcs_rhs", "fcs_tc",
            "fcs_jacobian", "fcs_rates", "fcs_bench_fp64_peak", "fcs_bench_fp32_peak", "fcs_check_exp",
            # include/fcs_mlp.h
            "fcs_mlp_create", "fcs_mlp_destroy", "fcs_mlp_last_error", "fcs_mlp_get_shape", "fcs_mlp_param_count",
@@ -121,6 +121,8 @@ def load(path: str = LIB) -> C.CDLL:
     L.fcs_integrate.argtypes = cell_args
     L.fcs_integrate_lts.argtypes = [vp, C.c_int64, vp] + cell_args[3:]
     L.fcs_integrate_noalloc.argtypes = cell_args[:-1]
+    L.fcs_integrate_async.argtypes = [vp, C.c_int64, C.c_double] + [vp] * 7 + [C.c_int32, vp]
+    L.fcs_sync.argtypes = [vp, C.POINTER(StepStats), _dp]
     L.fcs_rhs.argtypes = [vp, C.c_int64, vp, vp, vp, vp, C.c_int32]
     L.fcs_jacobian.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, C.c_int32]
     L.fcs_rates.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, vp, C.c_int32]
@@ -307,6 +309,21 @@ class Context:
         dmin = C.c_double(0)
         st = self.L.fcs_integrate_noalloc(self.h, n, dt, _addr(p), _addr(rho0), _addr(T), _addr(Y), _addr(sub),
                                           _addr(RR), _addr(status), C.byref(stats), C.byref(dmin))
+        if check and st not in (0, 5):
+            self._check(st)
+        return st, stats.as_dict(), dmin.value
+
+    def integrate_async(self, n, dt, p, rho0, T, Y, sub, RR=None, status=None, stream=None, flags=0):
+        """fcs_integrate_async on torch CUDA tensors; `stream` a torch.cuda.Stream (None: the context's)."""
+        st = self.L.fcs_integrate_async(self.h, n, dt, _addr(p), _addr(rho0), _addr(T), _addr(Y), _addr(sub),
+                                        _addr(RR), _addr(status), flags,
+                                        None if stream is None else stream.cuda_stream)
+        self._check(st)
+
+    def sync(self, check=True):
+        stats = StepStats()
+        dmin = C.c_double(0)
+        st = self.L.fcs_sync(self.h, C.byref(stats), C.byref(dmin))
         if check and st not in (0, 5):
             self._check(st)
         return st, stats.as_dict(), dmin.value

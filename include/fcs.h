@@ -219,6 +219,26 @@ fcs_status fcs_integrate(fcs_ctx* ctx, int64_t n_cells, double delta_t,
                          fcs_step_stats* stats, double* delta_t_min,
                          int32_t flags);
 
+/*
+ * fcs_integrate over caller-owned DEVICE arrays, enqueued on `cuda_stream`
+ * (a cudaStream_t of the context's device; NULL = the context's own stream)
+ * without waiting for it: the flow solver can overlap the chemistry with its
+ * own work, and order its next kernels after it on the same stream.  The
+ * step's results are in T, Y, sub_delta_t, RR, cell_status once the stream
+ * reaches them; fcs_sync waits for the step and returns its statistics and
+ * delta_t_min (same meaning as fcs_integrate's).  One step in flight per
+ * context: a second fcs_integrate_async before fcs_sync returns
+ * FCS_ERR_STATE.  The mapping is the option's, else one the autotuner already
+ * chose for this context, else the default (the autotuner needs a host round
+ * trip and is not run here).  flags: FCS_NO_QUEUE_SORT.
+ */
+fcs_status fcs_integrate_async(fcs_ctx* ctx, int64_t n_cells, double delta_t,
+                               const double* p, const double* rho0,
+                               double* T, double* Y, double* sub_delta_t,
+                               double* RR, int32_t* cell_status, int32_t flags,
+                               void* cuda_stream);
+fcs_status fcs_sync(fcs_ctx* ctx, fcs_step_stats* stats, double* delta_t_min);
+
 /* Same, with a per-cell delta_t (the local-time-stepping variant
  * FastChemistryModel::solve(const scalarField& deltaT),
  * FastChemistryModel_localEulerSolve.H:3-101). */

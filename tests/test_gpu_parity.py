@@ -339,3 +339,28 @@ def test_graph_step_recaptures_when_buffers_or_mechanism_change(built):
     ctx.set_options(abs_tol=w.abs_tol, rel_tol=w.rel_tol, mapping=64)
     T3, a3 = step()
     assert torch.equal(T1, T3) and a1 == a3
+
+
+def test_async_step_on_a_caller_stream_matches_integrate(built):
+    """fcs_integrate_async on a torch stream + fcs_sync equals fcs_integrate."""
+    import torch
+    w, mech, flat, c = _setup("counterflow_53s", 128)
+    ctx = _ctx(flat, abs_tol=w.abs_tol, rel_tol=w.rel_tol, mapping=64)
+    ref = ctx.integrate(c, w.dt)
+    d = {k: torch.from_numpy(np.ascontiguousarray(getattr(c, k))).cuda() for k in ("p", "rho0", "T", "Y", "subDt")}
+    RR = torch.zeros_like(d["Y"])
+    st = torch.zeros(c.n, dtype=torch.int32, device="cuda")
+    s = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    ctx.integrate_async(c.n, w.dt, d["p"], d["rho0"], d["T"], d["Y"], d["subDt"], RR, st, stream=s)
+    with pytest.raises(Exception):
+        ctx.integrate_async(c.n, w.dt, d["p"], d["rho0"], d["T"], d["Y"], d["subDt"], RR, st, stream=s)
+    code, stats, dmin = ctx.sync()
+    assert code == 0 and stats["cells_integrated"] == c.n
+    np.testing.assert_array_equal(d["T"].cpu().numpy(), ref["T"])
+    np.testing.assert_array_equal(d["Y"].cpu().numpy(), ref["Y"])
+    np.testing.assert_array_equal(RR.cpu().numpy(), ref["RR"])
+    assert dmin == ref["deltaTMin"] and stats["attempts"] == ref["stats"]["attempts"]
+    # host arrays are refused, not handed to the kernels
+    with pytest.raises(Exception):
+        ctx.integrate_async(c.n, w.dt, c.p, c.rho0, c.T.copy(), c.Y.copy(), c.subDt.copy())
