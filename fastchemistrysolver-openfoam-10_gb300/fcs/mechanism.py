@@ -302,7 +302,7 @@ def synthetic_mechanism(n_species: int, n_reactions: int, n_third_body: int,
                         n_plog: int, seed: int, n_elements: int = 3,
                         max_count: int = 3, plog_points: int = 5,
                         plog_p_range=(1e4, 1e8), hf_range_kJ=(-100.0, 100.0),
-                        name: Optional[str] = None) -> Mechanism:
+                        name: Optional[str] = None, n_falloff=(0, 0, 0)) -> Mechanism:
     """Build one seeded synthetic mechanism (all reactions reversible).
 
     The reactions are emitted in a shuffled *file* order so that the type
@@ -359,6 +359,29 @@ def synthetic_mechanism(n_species: int, n_reactions: int, n_third_body: int,
                          beta + bslope * x,
                          np.clip(Ta + tslope * x, 0.0, None)], axis=1)
         reactions.append(Reaction(PLOG, True, lr[0], lr[1], A, beta, Ta, plog=rows))
+    # fall-off (Lindemann, Troe, SRI): recombinations with k0 (per unit of M)
+    # above kInf so that Pr = k0 M / kInf crosses 1 over the fields' pressures
+    for kind, count in zip((LINDEMANN_FALLOFF, TROE_FALLOFF, SRI_FALLOFF), n_falloff):
+        for _ in range(count):
+            lr = builder.recombination() or builder.exchange()
+            if lr is None:
+                raise RuntimeError("could not close a fall-off template; change the seed")
+            lr = orient(lr)
+            A, beta, Ta = _arrhenius(rng)
+            A0 = A * 10.0 ** rng.uniform(1.0, 3.0)
+            beta0 = beta - rng.uniform(0.0, 1.5)
+            Ta0 = Ta * rng.uniform(0.0, 0.5)
+            eff = rng.uniform(0.5, 5.0, size=n_species)
+            if kind == TROE_FALLOFF:
+                fo = (rng.uniform(0.2, 0.9), rng.uniform(500.0, 5000.0), rng.uniform(2000.0, 10000.0),
+                      rng.uniform(50.0, 500.0))          # alpha, T*, T**, T***
+            elif kind == SRI_FALLOFF:
+                fo = (rng.uniform(0.5, 2.0), rng.uniform(100.0, 1000.0), rng.uniform(200.0, 2000.0),
+                      rng.uniform(0.8, 1.2), rng.uniform(-0.5, 0.5))  # a, b, c, d, e
+            else:
+                fo = None
+            reactions.append(Reaction(kind, True, lr[0], lr[1], A0 * T_REF_ARRHENIUS ** (beta - beta0), beta0, Ta0,
+                                      efficiencies=eff, kinf=(A, beta, Ta), falloff=fo))
     while len(reactions) < n_reactions:
         r = rng.random()
         lr = builder.exchange() if r < 0.8 else builder.recombination()

@@ -18,6 +18,10 @@ Workloads (all seeds fixed):
   cells: 80 % near-frozen (half of them below Treact = 700 K: T ~ U[300, 700),
   the other half T ~ U[700, 800]) and 20 % reacting (T ~ U[1200, 2200]),
   Y ~ Dirichlet(0.3), p ~ U[1e5, 1e6] Pa, dt = 5e-6 s.
+* ``falloff_16s`` -- 16 species / 48 reactions (3 third-body, 2 PLOG, 3 each of
+  Lindemann, Troe and SRI fall-off), 512 cells, T ~ U[900, 1800] K,
+  p log-uniform on [1e4, 1e7] Pa, Y ~ Dirichlet(0.5), dt = 1e-5 s: the parity
+  case of the fall-off kinds (no benchmark field uses them).
 * ``large_200s`` -- 200 species / 1,500 reactions (60 PLOG, 40 third-body),
   1,048,576 cells, T ~ U[600, 2400] K, p ~ U[1e5, 4e6] Pa, Y ~ Dirichlet(0.2),
   dt = 1e-5 s.
@@ -90,6 +94,10 @@ WORKLOADS = {
         "uneven_111s",
         dict(n_species=111, n_reactions=784, n_third_body=31, n_plog=0, seed=111),
         n_cells=262144, dt=5e-6, treact=700.0, cell_seed=111),
+    "falloff_16s": Workload(
+        "falloff_16s",
+        dict(n_species=16, n_reactions=48, n_third_body=3, n_plog=2, seed=1616, n_falloff=(3, 3, 3)),
+        n_cells=512, dt=1e-5, cell_seed=16),
     "large_200s": Workload(
         "large_200s",
         dict(n_species=200, n_reactions=1500, n_third_body=40, n_plog=60, seed=2000),
@@ -130,6 +138,10 @@ def cells_for(w: Workload, mech: Mechanism, n: Optional[int] = None,
                               rng.uniform(1200.0, 2200.0, n_full)))
         p = rng.uniform(1e5, 1e6, n_full)
         Y = rng.dirichlet(np.full(ns, 0.3), size=n_full).T
+    elif w.name == "falloff_16s":
+        T = rng.uniform(900.0, 1800.0, n_full)
+        p = 10.0 ** rng.uniform(4.0, 7.0, n_full)
+        Y = rng.dirichlet(np.full(ns, 0.5), size=n_full).T
     elif w.name == "large_200s":
         T = rng.uniform(600.0, 2400.0, n_full)
         p = rng.uniform(1e5, 4e6, n_full)

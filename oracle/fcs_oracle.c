@@ -42,7 +42,9 @@ struct orc_mech {
     /* per reaction, reference order */
     int *kind, *rev, *fileIdx, *lOff, *lSp, *rOff, *rSp, *tbRow, *plogIdx, *dnu;
     double *A, *beta, *Ta;
-    double *eff;                 /* [nTB][ns] */
+    double *A2, *beta2, *Ta2;    /* kInf of fall-off reactions (per reaction) */
+    double *fo;                  /* [nr][5] Troe (alpha, Ts, Tss, Tsss) / SRI (a, b, c, d, e) */
+    double *eff;                 /* [nTB][ns]: third-body rows, then fall-off rows */
     int *pOff;                   /* [nPlog+1] */
     double *pP, *pLogP, *pLogA, *pBeta, *pTa;
     int maxSp;
@@ -63,21 +65,23 @@ void orc_mech_destroy(orc_mech* m)
     free(m->kind); free(m->rev); free(m->fileIdx); free(m->lOff); free(m->lSp);
     free(m->rOff); free(m->rSp); free(m->tbRow); free(m->plogIdx); free(m->dnu);
     free(m->A); free(m->beta); free(m->Ta); free(m->eff); free(m->pOff);
+    free(m->A2); free(m->beta2); free(m->Ta2); free(m->fo);
     free(m->pP); free(m->pLogP); free(m->pLogA); free(m->pBeta); free(m->pTa);
     free(m);
 }
 
 /* Type-block order of OptReaction::readInfo (OptReaction.C:448-1175):
  * temperature-independent Arrhenius, other Arrhenius, (non-equilibrium),
- * third-body, fall-off, (chemically activated), PLOG; file order inside each
- * block. */
+ * third-body, fall-off (Lindemann, then Troe, then SRI: OptReaction.C:746-917),
+ * (chemically activated), PLOG; file order inside each block.  Fall-off
+ * reactions take third-body rows after the third-body reactions' (Itbr[2]). */
 orc_mech* orc_mech_create(const fcs_mechanism_desc* d, int32_t* status)
 {
     *status = FCS_OK;
     const int ns = d->n_species, nr = d->n_reactions;
     for (int r = 0; r < nr; r++) {
         int t = d->type[r];
-        if (t != FCS_RXN_ARRHENIUS && t != FCS_RXN_THIRD_BODY && t != FCS_RXN_PLOG) {
+        if (t < FCS_RXN_ARRHENIUS || t > FCS_RXN_SRI_FALLOFF) {
             *status = FCS_ERR_UNSUPPORTED;
             return NULL;
         }
@@ -102,7 +106,7 @@ orc_mech* orc_mech_create(const fcs_mechanism_desc* d, int32_t* status)
     }
     int* order = (int*)malloc(sizeof(int) * (nr > 0 ? nr : 1));
     int k = 0;
-    for (int pass = 0; pass < 4; pass++) {
+    for (int pass = 0; pass < 7; pass++) {
         for (int r = 0; r < nr; r++) {
             int t = d->type[r];
             double beta = d->arrhenius[3 * r + 1], Ta = d->arrhenius[3 * r + 2];
@@ -110,7 +114,10 @@ orc_mech* orc_mech_create(const fcs_mechanism_desc* d, int32_t* status)
             if ((pass == 0 && t == FCS_RXN_ARRHENIUS && tind) ||
                 (pass == 1 && t == FCS_RXN_ARRHENIUS && !tind) ||
                 (pass == 2 && t == FCS_RXN_THIRD_BODY) ||
-                (pass == 3 && t == FCS_RXN_PLOG))
+                (pass == 3 && t == FCS_RXN_LINDEMANN_FALLOFF) ||
+                (pass == 4 && t == FCS_RXN_TROE_FALLOFF) ||
+                (pass == 5 && t == FCS_RXN_SRI_FALLOFF) ||
+                (pass == 6 && t == FCS_RXN_PLOG))
                 order[k++] = r;
         }
     }
@@ -120,11 +127,13 @@ orc_mech* orc_mech_create(const fcs_mechanism_desc* d, int32_t* status)
     ALLOC_I(m->lOff, nr + 1); ALLOC_I(m->rOff, nr + 1); ALLOC_I(m->tbRow, nr);
     ALLOC_I(m->plogIdx, nr); ALLOC_I(m->dnu, nr);
     ALLOC_D(m->A, nr); ALLOC_D(m->beta, nr); ALLOC_D(m->Ta, nr);
+    ALLOC_D(m->A2, nr); ALLOC_D(m->beta2, nr); ALLOC_D(m->Ta2, nr); ALLOC_D(m->fo, (size_t)nr * 5);
     int nl_tot = d->lhs_offset[nr], nr_tot = d->rhs_offset[nr];
     ALLOC_I(m->lSp, nl_tot); ALLOC_I(m->rSp, nr_tot);
     int nTB = 0, nPlog = 0, plogRows = 0;
     for (int r = 0; r < nr; r++) {
-        if (d->type[r] == FCS_RXN_THIRD_BODY) nTB++;
+        if (d->type[r] == FCS_RXN_THIRD_BODY || d->type[r] >= FCS_RXN_LINDEMANN_FALLOFF) nTB++;
+        if (d->type[r] >= FCS_RXN_LINDEMANN_FALLOFF) m->nFO++;
         if (d->type[r] == FCS_RXN_PLOG) { nPlog++; plogRows += d->plog_offset[r + 1] - d->plog_offset[r]; }
     }
     m->nTB = nTB; m->nPlog = nPlog;
@@ -153,9 +162,15 @@ orc_mech* orc_mech_create(const fcs_mechanism_desc* d, int32_t* status)
         m->dnu[i] = nrr - nlr;
         m->tbRow[i] = -1;
         m->plogIdx[i] = -1;
-        if (m->kind[i] == FCS_RXN_THIRD_BODY) {
+        if (m->kind[i] == FCS_RXN_THIRD_BODY || m->kind[i] >= FCS_RXN_LINDEMANN_FALLOFF) {
             for (int s = 0; s < ns; s++) m->eff[tb * ns + s] = d->efficiencies[(size_t)r * ns + s];
             m->tbRow[i] = tb++;
+        }
+        if (m->kind[i] >= FCS_RXN_LINDEMANN_FALLOFF) {
+            m->A2[i] = d->arrhenius2[3 * r + 0];
+            m->beta2[i] = d->arrhenius2[3 * r + 1];
+            m->Ta2[i] = d->arrhenius2[3 * r + 2];
+            for (int q = 0; q < 5; q++) m->fo[(size_t)i * 5 + q] = d->falloff_params[(size_t)r * 5 + q];
         }
         if (m->kind[i] == FCS_RXN_PLOG) {
             m->plogIdx[i] = pl;
@@ -190,6 +205,7 @@ typedef struct {
     int n;
     double *C, *B, *dBdT, *Cp, *Ha, *dCpdT, *rhoMvj, *WiByrhoM;
     double *Kf, *dKfdT, *M, *Kplog, *dKplog;
+    double *Kinf, *dKinfdT;      /* kInf of fall-off reactions */
     double *Jc, *Jy, *a;       /* N*N each */
     double *vec[16];           /* N each */
     int *piv;
@@ -213,6 +229,8 @@ static ws_t* ws_create(const orc_mech* m)
     w->dCpdT = (double*)calloc(ns, sizeof(double));
     w->rhoMvj = (double*)calloc(ns, sizeof(double));
     w->WiByrhoM = (double*)calloc(ns, sizeof(double));
+    w->Kinf = (double*)calloc(nr + 1, sizeof(double));
+    w->dKinfdT = (double*)calloc(nr + 1, sizeof(double));
     w->Kf = (double*)calloc(nr + 1, sizeof(double));
     w->dKfdT = (double*)calloc(nr + 1, sizeof(double));
     w->M = (double*)calloc(m->nTB + 1, sizeof(double));
@@ -232,6 +250,7 @@ static void ws_destroy(ws_t* w)
 {
     free(w->C); free(w->B); free(w->dBdT); free(w->Cp); free(w->Ha); free(w->dCpdT);
     free(w->rhoMvj); free(w->WiByrhoM); free(w->Kf); free(w->dKfdT); free(w->M);
+    free(w->Kinf); free(w->dKinfdT);
     free(w->Kplog); free(w->dKplog); free(w->Jc); free(w->Jy); free(w->a);
     for (int i = 0; i < 16; i++) free(w->vec[i]);
     free(w->piv); free(w->invD); free(w->table);
@@ -325,7 +344,111 @@ static void arrhenius_rates(const orc_mech* m, ws_t* w, double logT, double invT
         const double k = m->A[i] * exp(fma(m->beta[i], logT, -(m->Ta[i] * invT)));
         w->Kf[i] = k;
         if (withDeriv) w->dKfdT[i] = k * (fma(m->Ta[i], invT, m->beta[i]) * invT);
+        if (m->kind[i] >= FCS_RXN_LINDEMANN_FALLOFF) {
+            /* kInf sits at Ikf[7] + (i - Ikf[4]) in the reference's Kf_ (OptReaction.C:768-772) */
+            const double ki = m->A2[i] * exp(fma(m->beta2[i], logT, -(m->Ta2[i] * invT)));
+            w->Kinf[i] = ki;
+            if (withDeriv) w->dKinfdT[i] = ki * (fma(m->Ta2[i], invT, m->beta2[i]) * invT);
+        }
     }
+}
+
+/* Fall-off rate of reaction i from K0 = Kf[i], kInf and M (ReactionRate.C:370-519,
+ * pressureReactionFunctionI.H Troe_F_1..3 / SRI_F): Kf = M K0 F / (1 + Pr),
+ * Pr = K0 M / kInf, F = 1 (Lindemann), Troe or SRI.  T is the clamped
+ * temperature.  With dKfdT / dKfdC (Jacobian.C:426-713, Troe_Jac_1..3,
+ * SRI_F_dFdT_dFdPr) also d/dT and d/dM; note that the SRI branch of the
+ * reference uses dF/dT at fixed Pr (no dF/dPr dPr/dT term) and the Troe
+ * branch the total derivative. */
+static double falloff_rate(const orc_mech* m, const ws_t* w, int i, double T, double invT, double* dKfdT,
+                           double* dKfdC)
+{
+    const double K0 = w->Kf[i], Kinf = w->Kinf[i], M = w->M[m->tbRow[i]];
+    const double* f = &m->fo[(size_t)i * 5];
+    if (m->kind[i] == FCS_RXN_LINDEMANN_FALLOFF) {
+        if (!dKfdT) {
+            const double Pr = (K0 * M) / Kinf;
+            const double N = K0 / (Pr + 1.0);
+            return M * N;
+        }
+        const double invKinf = 1.0 / Kinf;
+        const double Pr = (K0 * M) * invKinf;
+        const double dPrdT = fma(M, w->dKfdT[i], -(Pr * w->dKinfdT[i])) * invKinf;
+        const double tmp = 1.0 / (1.0 + Pr);
+        const double dKdT = Pr * w->dKinfdT[i];
+        *dKfdT = fma(tmp, dKdT, ((tmp * tmp) * dPrdT) * Kinf);
+        *dKfdC = (K0 * tmp) * tmp;
+        return M * (tmp * K0);
+    }
+    const double Pr = K0 * M / Kinf;
+    const double logPr = log10(fmax(Pr, SMALL));
+    double F, dFdT = 0, dFdPr = 0;
+    if (m->kind[i] == FCS_RXN_TROE_FALLOFF) {
+        const double alpha = f[0], Ts = f[1], Tss = f[2], Tsss = f[3];
+        const double expTTsss = exp(-T * (1.0 / Tsss)), expTTss = exp(-Tss * invT), expTTs = exp(-T * (1.0 / Ts));
+        const double Fcent = (1 - alpha) * expTTsss + alpha * expTTs + expTTss;
+        const double logFcent = log10(fmax(Fcent, SMALL));
+        const double c = -0.4 - 0.67 * logFcent;
+        const double n = 0.75 - 1.27 * logFcent;
+        const double x1 = n - 0.14 * (logPr + c);
+        if (!dKfdT) {
+            const double x2 = (logPr + c) / x1;
+            const double x3 = 1 + (x2 * x2);
+            F = pow(10, logFcent / x3);
+        } else {
+            const double invx1 = 1.0 / x1;
+            const double x2 = (logPr + c) * invx1;
+            const double x3 = 1 + (x2 * x2);
+            const double invx3 = 1.0 / x3;
+            const double x4 = logFcent * invx3;
+            F = pow(10, x4);
+            const double logTen = log(10.0);
+            const double dFcentdT = -(1 - alpha) * (1.0 / Tsss) * expTTsss - alpha * (1.0 / Ts) * expTTs
+                                    + Tss * invT * invT * expTTss;
+            const double dlogFcentdT = Fcent >= SMALL ? dFcentdT / Fcent / logTen : 0;
+            const double dcdT = -0.67 * dlogFcentdT;
+            const double dndT = -1.27 * dlogFcentdT;
+            const double dx1dT = dndT - 0.14 * dcdT;
+            const double dx2dT = (dcdT - x2 * dx1dT) * invx1;
+            const double dx3dT = 2 * x2 * dx2dT;
+            const double dx4dT = (dlogFcentdT - x4 * dx3dT) * invx3;
+            const double dlogPrdPr = Pr >= SMALL ? 1 / (logTen * Pr) : 0;
+            const double dx1dPr = -0.14 * dlogPrdPr;
+            const double dx2dPr = (dlogPrdPr - x2 * dx1dPr) * invx1;
+            const double dx3dPr = 2 * x2 * dx2dPr;
+            const double dx4dPr = -x4 * dx3dPr * invx3;
+            dFdPr = logTen * F * dx4dPr;
+            const double dPrdT = (M * w->dKfdT[i] - Pr * w->dKinfdT[i]) * (1.0 / Kinf);
+            dFdT = logTen * F * dx4dT + dFdPr * dPrdT;
+        }
+    } else {
+        const double a = f[0], b = f[1], c = f[2], d = f[3], e = f[4];
+        const double X = 1 / (1 + (logPr * logPr));
+        if (!dKfdT) {
+            const double psi = a * exp(-b / T) + exp(-T / c);
+            F = d * pow(psi, X) * pow(T, e);
+        } else {
+            const double expbT = exp(-b * invT), expTc = exp(-T * (1.0 / c));
+            const double psi = a * expbT + expTc;
+            F = d * pow(psi, X) * pow(T, e);
+            const double dpsidT = a * b / (T * T) * expbT - 1 / c * expTc;
+            dFdT = F * (X / psi * dpsidT + e / T);
+            const double logTen = log(10.0);
+            const double dlogPrdPr = Pr >= SMALL ? 1 / (logTen * Pr) : 0;
+            const double dXdPr = -(X * X) * 2 * logPr * dlogPrdPr;
+            dFdPr = F * log(psi) * dXdPr;
+        }
+    }
+    const double invOnePlusPr = 1.0 / (1 + Pr);
+    if (dKfdT) {
+        const double invKinf = 1.0 / Kinf;
+        const double dPrdT = (M * w->dKfdT[i] - Pr * w->dKinfdT[i]) * invKinf;
+        const double dKdT = Pr * w->dKinfdT[i];
+        *dKfdT = F * invOnePlusPr * dKdT + F * invOnePlusPr * invOnePlusPr * dPrdT * Kinf
+                 + K0 * invOnePlusPr * dFdT * M;
+        *dKfdC = K0 * invOnePlusPr * 1.0 * (F * invOnePlusPr + Pr * dFdPr);
+    }
+    return M * (invOnePlusPr * F * K0);
 }
 
 static void third_body(const orc_mech* m, ws_t* w)
@@ -400,8 +523,10 @@ static void dNdtByV(const orc_mech* m, ws_t* w, double p, double T, double* omeg
     const double PByRT = PSTD / (RU * Tc);
     arrhenius_rates(m, w, logT, invT, 0);
     third_body(m, w);
-    for (int i = 0; i < m->nr; i++)
+    for (int i = 0; i < m->nr; i++) {
         if (m->kind[i] == FCS_RXN_THIRD_BODY) w->Kf[i] *= w->M[m->tbRow[i]];
+        else if (m->kind[i] >= FCS_RXN_LINDEMANN_FALLOFF) w->Kf[i] = falloff_rate(m, w, i, Tc, invT, NULL, NULL);
+    }
     if (m->nPlog) plog_rates(m, w, p, logT, invT, 0);
     memset(omega, 0, sizeof(double) * ns);
     for (int i = 0; i < m->nr; i++) {
@@ -499,7 +624,9 @@ static void jacobian(const orc_mech* m, ws_t* w, const orc_options* o, double p,
         int tb = m->tbRow[i];
         if (m->kind[i] == FCS_RXN_PLOG) { Kf = w->Kplog[m->plogIdx[i]]; dKfdT = w->dKplog[m->plogIdx[i]]; }
         else { Kf = w->Kf[i]; dKfdT = w->dKfdT[i]; }
-        if (tb >= 0) {
+        if (m->kind[i] >= FCS_RXN_LINDEMANN_FALLOFF) {
+            Kf = falloff_rate(m, w, i, Tc, invT, &dKfdT, &dKfdC);
+        } else if (tb >= 0) {
             /* Jacobian.C:401-420: dKf/dM = Kf(before M), Kf *= M, dKf/dT *= M */
             dKfdC = Kf;
             Kf *= w->M[tb];
@@ -1405,8 +1532,10 @@ int32_t orc_tc(const orc_mech* m, int64_t n_cells, const double* p, const double
         const double PByRT = PSTD / (RU * Tc);
         arrhenius_rates(m, w, logT, invT, 0);
         third_body(m, w);
-        for (int i = 0; i < m->nr; i++)
+        for (int i = 0; i < m->nr; i++) {
             if (m->kind[i] == FCS_RXN_THIRD_BODY) w->Kf[i] *= w->M[m->tbRow[i]];
+            else if (m->kind[i] >= FCS_RXN_LINDEMANN_FALLOFF) w->Kf[i] = falloff_rate(m, w, i, Tc, invT, NULL, NULL);
+        }
         if (m->nPlog) plog_rates(m, w, p[c], logT, invT, 0);
         double sumW = 0, sumWR = 0;
         for (int i = 0; i < m->nr; i++) {

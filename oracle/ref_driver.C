@@ -56,6 +56,7 @@ void fill_reaction(OptReaction& R, const fcs_mechanism_desc* d)
         if (d->type[r] == FCS_RXN_ARRHENIUS) R.n_Arrhenius++;
         else if (d->type[r] == FCS_RXN_THIRD_BODY) R.n_ThirdBodyReaction++;
         else if (d->type[r] == FCS_RXN_PLOG) R.n_PlogReaction++;
+        else if (d->type[r] >= FCS_RXN_LINDEMANN_FALLOFF && d->type[r] <= FCS_RXN_SRI_FALLOFF) R.n_Fall_Off_Reaction++;
         else throw std::runtime_error("unsupported reaction type in reference driver");
     }
     R.Itbr[0] = 0;
@@ -142,6 +143,48 @@ void fill_reaction(OptReaction& R, const fcs_mechanism_desc* d)
         species(r, iA);
         iA++; k++;
     }
+    // fall-off reactions: Lindemann, then Troe, then SRI (OptReaction.C:746-917); k0 at
+    // the reaction's slot, kInf at Ikf[7] + (slot - Ikf[4]), a third-body row each
+    for (int kind : {FCS_RXN_LINDEMANN_FALLOFF, FCS_RXN_TROE_FALLOFF, FCS_RXN_SRI_FALLOFF}) {
+        for (unsigned r = 0; r < nr; r++) {
+            if (d->type[r] != kind) continue;
+            if (!d->reversible[r]) R.isIrreversible[iA] = 1;
+            R.A[iA] = d->arrhenius[3 * r];
+            R.beta[iA] = d->arrhenius[3 * r + 1];
+            R.Ta[iA] = d->arrhenius[3 * r + 2];
+            const unsigned begin = iA - R.Ikf[4] + R.Ikf[7];
+            R.A[begin] = d->arrhenius2[3 * r];
+            R.beta[begin] = d->arrhenius2[3 * r + 1];
+            R.Ta[begin] = d->arrhenius2[3 * r + 2];
+            R.ThirdBodyFactor[k].resize(ns);
+            for (unsigned s = 0; s < ns; s++) R.ThirdBodyFactor[k][s] = d->efficiencies[(size_t)r * ns + s];
+            const double* f = &d->falloff_params[(size_t)r * 5];
+            if (kind == FCS_RXN_LINDEMANN_FALLOFF) {
+                R.Lindemann.push_back(iA);
+            } else if (kind == FCS_RXN_TROE_FALLOFF) {
+                R.Troe.push_back(iA);
+                R.alpha_.push_back(f[0]);
+                R.Ts_.push_back(f[1]);
+                R.Tss_.push_back(f[2]);
+                R.Tsss_.push_back(f[3]);
+            } else {
+                R.SRI.push_back(iA);
+                R.a_.push_back(f[0]);
+                R.b_.push_back(f[1]);
+                R.c_.push_back(f[2]);
+                R.d_.push_back(f[3]);
+                R.e_.push_back(f[4]);
+            }
+            species(r, iA);
+            iA++; k++;
+        }
+    }
+    R.invTs_.resize(R.Ts_.size());
+    R.invTsss_.resize(R.Tsss_.size());
+    for (size_t i = 0; i < R.Ts_.size(); i++) R.invTs_[i] = 1.0 / R.Ts_[i];
+    for (size_t i = 0; i < R.Tsss_.size(); i++) R.invTsss_[i] = 1.0 / R.Tsss_[i];
+    R.invc_.resize(R.c_.size());
+    for (size_t i = 0; i < R.c_.size(); i++) R.invc_[i] = 1.0 / R.c_[i];
     R.ThirdBodyFactor1D.resize(R.ThirdBodyFactor.size() * ns);
     {
         unsigned c = 0;
@@ -366,7 +409,7 @@ template<class S> struct SolverT : Solver {
 struct RefHandle {
     fcs_mechanism_desc desc;
     // deep copies of the description arrays
-    std::vector<double> W, Tl, Th, Tc, hc, lc, arr, eff, pt;
+    std::vector<double> W, Tl, Th, Tc, hc, lc, arr, arr2, fo, eff, pt;
     std::vector<int32_t> type, rev, lo, ls, ro, rs, po;
     int solver, jacobian, maxSteps;
     double absTol, relTol;
@@ -406,6 +449,10 @@ void* ref_create(const fcs_mechanism_desc* d, int solver, int jacobian, double a
     h->arr.assign(d->arrhenius, d->arrhenius + 3 * nr);
     if (d->efficiencies) h->eff.assign(d->efficiencies, d->efficiencies + (size_t)nr * ns);
     else h->eff.assign((size_t)nr * ns, 1.0);
+    if (d->arrhenius2) h->arr2.assign(d->arrhenius2, d->arrhenius2 + 3 * nr);
+    else h->arr2.assign(3 * (size_t)nr, 0.0);
+    if (d->falloff_params) h->fo.assign(d->falloff_params, d->falloff_params + 5 * (size_t)nr);
+    else h->fo.assign(5 * (size_t)nr, 0.0);
     h->po.assign(d->plog_offset, d->plog_offset + nr + 1);
     h->pt.assign(d->plog_table, d->plog_table + 4 * (size_t)d->plog_offset[nr]);
     fcs_mechanism_desc& c = h->desc;
@@ -417,9 +464,10 @@ void* ref_create(const fcs_mechanism_desc* d, int solver, int jacobian, double a
     c.lhs_offset = h->lo.data(); c.lhs_species = h->ls.data();
     c.rhs_offset = h->ro.data(); c.rhs_species = h->rs.data();
     c.arrhenius = h->arr.data(); c.efficiencies = h->eff.data();
+    c.arrhenius2 = h->arr2.data(); c.falloff_params = h->fo.data();
     c.plog_offset = h->po.data(); c.plog_table = h->pt.data();
     for (int r = 0; r < nr; r++)
-        if (d->type[r] != FCS_RXN_ARRHENIUS && d->type[r] != FCS_RXN_THIRD_BODY && d->type[r] != FCS_RXN_PLOG) {
+        if (d->type[r] < FCS_RXN_ARRHENIUS || d->type[r] > FCS_RXN_SRI_FALLOFF) {
             delete h;
             return nullptr;
         }
