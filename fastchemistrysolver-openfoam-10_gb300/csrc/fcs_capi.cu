@@ -78,7 +78,7 @@ extern "C" fcs_status fcs_destroy(fcs_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     gate_release(ctx);
     for (DBuf<double>* b : {&ctx->dW, &ctx->dInvW, &ctx->dTc, &ctx->dCoef, &ctx->dEff, &ctx->dPlogRow,
-                            &ctx->dPlogTa, &ctx->dHf, &ctx->bp, &ctx->brho, &ctx->bT, &ctx->bY,
+                            &ctx->dPlogTa, &ctx->dHf, &ctx->dFo, &ctx->bp, &ctx->brho, &ctx->bT, &ctx->bY,
                             &ctx->bSub, &ctx->bRR, &ctx->bDt, &ctx->bOut, &ctx->bJ, &ctx->bQ})
         b->release();
     ctx->dRx.release();
@@ -137,19 +137,23 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
                    !d->rhs_species || !d->arrhenius))
         return set_err(ctx, FCS_ERR_INVALID, "missing reaction arrays");
     std::vector<int> order;
-    for (int pass = 0; pass < 4; pass++) {
+    // type blocks: T-independent Arrhenius, Arrhenius, third body, fall-off
+    // (Lindemann, Troe, SRI: OptReaction.C:746-917), PLOG
+    for (int pass = 0; pass < 7; pass++) {
         for (int r = 0; r < nr; r++) {
             const int t = d->type[r];
             const bool tind = d->arrhenius[3 * r + 1] == 0 && d->arrhenius[3 * r + 2] == 0;
             if ((pass == 0 && t == FCS_RXN_ARRHENIUS && tind) || (pass == 1 && t == FCS_RXN_ARRHENIUS && !tind) ||
-                (pass == 2 && t == FCS_RXN_THIRD_BODY) || (pass == 3 && t == FCS_RXN_PLOG))
+                (pass == 2 && t == FCS_RXN_THIRD_BODY) || (pass == 3 && t == FCS_RXN_LINDEMANN_FALLOFF) ||
+                (pass == 4 && t == FCS_RXN_TROE_FALLOFF) || (pass == 5 && t == FCS_RXN_SRI_FALLOFF) ||
+                (pass == 6 && t == FCS_RXN_PLOG))
                 order.push_back(r);
         }
     }
     if ((int)order.size() != nr)
         return set_err(ctx, FCS_ERR_UNSUPPORTED,
-                       "reaction types other than (ir)reversible Arrhenius, ThirdBodyArrhenius and "
-                       "ArrheniusPLOG are not supported by the GPU path");
+                       "reaction types other than (ir)reversible Arrhenius, ThirdBodyArrhenius, "
+                       "ArrheniusLindemann/Troe/SRIFallOff and ArrheniusPLOG are not supported by the GPU path");
     std::vector<double> W(ns), invW(ns), Tc(ns), coef(16 * (size_t)ns, 0.0), hf(ns);
     double TlowMin = 1e10, ThighMax = 1, TcMin = 1e10, TcMax = 0;
     for (int i = 0; i < ns; i++) {
@@ -174,7 +178,7 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
     std::vector<RxnInfo> rx(std::max(nr, 1));
     std::vector<double> eff;
     std::vector<int> plogOff{0};
-    std::vector<double> plogRow, plogTa;
+    std::vector<double> plogRow, plogTa, fo;
     std::vector<std::vector<int>> inc(ns);
     std::vector<int> tbInc;
     int nTB = 0, nPlog = 0;
@@ -212,7 +216,17 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
         x.tind = (x.beta == 0 && x.Ta == 0) ? 1 : 0;
         x.tb = -1;
         x.plog = -1;
-        if (d->type[r] == FCS_RXN_THIRD_BODY) {
+        x.fo = -1;
+        const bool falloff = d->type[r] >= FCS_RXN_LINDEMANN_FALLOFF && d->type[r] <= FCS_RXN_SRI_FALLOFF;
+        if (falloff) {
+            if (!d->arrhenius2) return set_err(ctx, FCS_ERR_INVALID, "fall-off reaction without kInf (arrhenius2)");
+            if (d->type[r] != FCS_RXN_LINDEMANN_FALLOFF && !d->falloff_params)
+                return set_err(ctx, FCS_ERR_INVALID, "Troe/SRI reaction without falloff_params");
+            x.fo = (int)(fo.size() / 8);
+            for (int q = 0; q < 3; q++) fo.push_back(d->arrhenius2[3 * (size_t)r + q]);
+            for (int q = 0; q < 5; q++) fo.push_back(d->falloff_params ? d->falloff_params[5 * (size_t)r + q] : 0.0);
+        }
+        if (d->type[r] == FCS_RXN_THIRD_BODY || falloff) {
             if (!d->efficiencies) return set_err(ctx, FCS_ERR_INVALID, "third-body reaction without efficiencies");
             for (int s = 0; s < ns; s++) eff.push_back(d->efficiencies[(size_t)r * ns + s]);
             x.tb = nTB++;
@@ -247,6 +261,7 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
     if (nTB >= 32768) return set_err(ctx, FCS_ERR_UNSUPPORTED, "too many third-body reactions");
     if (eff.empty()) eff.push_back(0);
     if (plogRow.empty()) { plogRow.assign(4, 0); plogTa.assign(1, 0); }
+    if (fo.empty()) fo.assign(8, 0.0);
     cudaSetDevice(ctx->device);
     auto up = [&](auto& buf, const auto& v) -> cudaError_t {
         cudaError_t e = buf.ensure(v.size());
@@ -256,7 +271,7 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
     CK(up(ctx->dW, W)); CK(up(ctx->dInvW, invW)); CK(up(ctx->dTc, Tc)); CK(up(ctx->dCoef, coef));
     CK(up(ctx->dRx, rx)); CK(up(ctx->dEff, eff)); CK(up(ctx->dPlogOff, plogOff));
     CK(up(ctx->dPlogRow, plogRow)); CK(up(ctx->dPlogTa, plogTa)); CK(up(ctx->dIncOff, incOff));
-    CK(up(ctx->dInc, incv)); CK(up(ctx->dHf, hf)); CK(up(ctx->dTbInc, tbInc));
+    CK(up(ctx->dInc, incv)); CK(up(ctx->dHf, hf)); CK(up(ctx->dTbInc, tbInc)); CK(up(ctx->dFo, fo));
     DevMech& M = ctx->M;
     M.ns = ns; M.n = ns + 1; M.nr = nr; M.nTB = nTB; M.nPlog = nPlog;
     M.TlowMin = TlowMin; M.ThighMax = ThighMax; M.TcommonMin = TcMin; M.TcommonMax = TcMax;
@@ -264,6 +279,14 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
     M.rx = ctx->dRx.p; M.eff = ctx->dEff.p; M.plogOff = ctx->dPlogOff.p; M.plogRow = ctx->dPlogRow.p;
     M.plogTa = ctx->dPlogTa.p; M.incOff = ctx->dIncOff.p; M.inc = ctx->dInc.p; M.hf = ctx->dHf.p;
     M.nTbInc = nTbInc; M.tbInc = ctx->dTbInc.p;
+    M.fo = ctx->dFo.p;
+    M.foBegin = 0;
+    M.nFo = 0;
+    for (int k = 0; k < nr; k++)
+        if (rx[k].fo >= 0) {
+            if (M.nFo == 0) M.foBegin = k;
+            M.nFo++;
+        }
     ctx->loaded = true;
     ctx->tuned.clear();
     if (ctx->gexec) {  // a captured step holds the old mechanism's scalars

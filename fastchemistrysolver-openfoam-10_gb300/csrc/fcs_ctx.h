@@ -70,7 +70,7 @@ struct fcs_ctx {
     // mechanism
     bool loaded = false;
     fcs::DevMech M{};
-    fcs::DBuf<double> dW, dInvW, dTc, dCoef, dEff, dPlogRow, dPlogTa, dHf;
+    fcs::DBuf<double> dW, dInvW, dTc, dCoef, dEff, dPlogRow, dPlogTa, dHf, dFo;
     fcs::DBuf<fcs::RxnInfo> dRx;
     fcs::DBuf<int> dPlogOff, dIncOff, dInc, dTbInc;
     // options

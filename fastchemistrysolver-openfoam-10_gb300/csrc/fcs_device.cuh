@@ -429,6 +429,102 @@ __device__ __forceinline__ RxnInfo load_rx(const RxnInfo* p) {
 }
 
 // ------------------------------------------------------------------------
+// fall-off reactions (ReactionRate.C:370-519, Jacobian.C:426-713,
+// pressureReactionFunctionI.H): Kf = M K0 F / (1 + Pr), Pr = K0 M / kInf,
+// F = 1 (Lindemann), Troe or SRI.  K0 is the reaction's own Arrhenius rate,
+// kInf and the F parameters come from DevMech::fo; Tc is the clamped
+// temperature.  With deriv, also dKf/dT and dKf/dM; the SRI branch uses dF/dT
+// at fixed Pr, as the reference does (no dF/dPr dPr/dT term), the Troe branch
+// the total derivative.
+
+struct FalloffK { double Kf, dKfdT, dKfdC; };
+
+static __device__ __noinline__ FalloffK falloff_rate(const DevMech& M, const RxnInfo& x, double K0, double dK0dT,
+                                                     double Mt, double Tc, double logT, double invT, bool deriv) {
+    const double* f = M.fo + (size_t)x.fo * 8;
+    const double A2 = __ldg(f), b2 = __ldg(f + 1), Ta2 = __ldg(f + 2);
+    const double Kinf = A2 * fast_exp(fma(b2, logT, -(Ta2 * invT)));
+    const double dKinfdT = Kinf * (fma(Ta2, invT, b2) * invT);
+    FalloffK o{0, 0, 0};
+    if (x.kind == FCS_RXN_LINDEMANN_FALLOFF) {
+        if (!deriv) {
+            const double Pr = (K0 * Mt) / Kinf;
+            o.Kf = Mt * (K0 / (Pr + 1.0));
+            return o;
+        }
+        const double invKinf = 1.0 / Kinf;
+        const double Pr = (K0 * Mt) * invKinf;
+        const double dPrdT = fma(Mt, dK0dT, -(Pr * dKinfdT)) * invKinf;
+        const double tmp = 1.0 / (1.0 + Pr);
+        o.dKfdT = fma(tmp, Pr * dKinfdT, ((tmp * tmp) * dPrdT) * Kinf);
+        o.dKfdC = (K0 * tmp) * tmp;
+        o.Kf = Mt * (tmp * K0);
+        return o;
+    }
+    const double small = 1e-15;
+    const double Pr = K0 * Mt / Kinf;
+    const double logPr = log10(fmax(Pr, small));
+    const double logTen = 2.302585092994045684;
+    double F, dFdT = 0, dFdPr = 0;
+    if (x.kind == FCS_RXN_TROE_FALLOFF) {
+        const double alpha = __ldg(f + 3), Ts = __ldg(f + 4), Tss = __ldg(f + 5), Tsss = __ldg(f + 6);
+        const double invTsss = 1.0 / Tsss, invTs = 1.0 / Ts;
+        const double eTsss = fast_exp(-Tc * invTsss), eTss = fast_exp(-Tss * invT), eTs = fast_exp(-Tc * invTs);
+        const double Fcent = (1 - alpha) * eTsss + alpha * eTs + eTss;
+        const double logFcent = log10(fmax(Fcent, small));
+        const double c = -0.4 - 0.67 * logFcent;
+        const double n = 0.75 - 1.27 * logFcent;
+        const double x1 = n - 0.14 * (logPr + c);
+        const double invx1 = 1.0 / x1;
+        const double x2 = (logPr + c) * invx1;
+        const double x3 = 1 + (x2 * x2);
+        const double invx3 = 1.0 / x3;
+        const double x4 = logFcent * invx3;
+        F = pow(10.0, x4);
+        if (deriv) {
+            const double dFcentdT = -(1 - alpha) * invTsss * eTsss - alpha * invTs * eTs + Tss * invT * invT * eTss;
+            const double dlogFcentdT = Fcent >= small ? dFcentdT / Fcent / logTen : 0;
+            const double dcdT = -0.67 * dlogFcentdT;
+            const double dndT = -1.27 * dlogFcentdT;
+            const double dx1dT = dndT - 0.14 * dcdT;
+            const double dx2dT = (dcdT - x2 * dx1dT) * invx1;
+            const double dx3dT = 2 * x2 * dx2dT;
+            const double dx4dT = (dlogFcentdT - x4 * dx3dT) * invx3;
+            const double dlogPrdPr = Pr >= small ? 1 / (logTen * Pr) : 0;
+            const double dx1dPr = -0.14 * dlogPrdPr;
+            const double dx2dPr = (dlogPrdPr - x2 * dx1dPr) * invx1;
+            const double dx3dPr = 2 * x2 * dx2dPr;
+            const double dx4dPr = -x4 * dx3dPr * invx3;
+            dFdPr = logTen * F * dx4dPr;
+            const double dPrdT = (Mt * dK0dT - Pr * dKinfdT) * (1.0 / Kinf);
+            dFdT = logTen * F * dx4dT + dFdPr * dPrdT;
+        }
+    } else {
+        const double a = __ldg(f + 3), b = __ldg(f + 4), c = __ldg(f + 5), d = __ldg(f + 6), e = __ldg(f + 7);
+        const double X = 1 / (1 + (logPr * logPr));
+        const double eb = fast_exp(-b * invT), ec = fast_exp(-Tc * (1.0 / c));
+        const double psi = a * eb + ec;
+        F = d * pow(psi, X) * pow(Tc, e);
+        if (deriv) {
+            const double dpsidT = a * b / (Tc * Tc) * eb - 1 / c * ec;
+            dFdT = F * (X / psi * dpsidT + e / Tc);
+            const double dlogPrdPr = Pr >= small ? 1 / (logTen * Pr) : 0;
+            const double dXdPr = -(X * X) * 2 * logPr * dlogPrdPr;
+            dFdPr = F * log(psi) * dXdPr;
+        }
+    }
+    const double invOnePlusPr = 1.0 / (1 + Pr);
+    if (deriv) {
+        const double dPrdT = (Mt * dK0dT - Pr * dKinfdT) * (1.0 / Kinf);
+        o.dKfdT = F * invOnePlusPr * (Pr * dKinfdT) + F * invOnePlusPr * invOnePlusPr * dPrdT * Kinf +
+                  K0 * invOnePlusPr * dFdT * Mt;
+        o.dKfdC = K0 * invOnePlusPr * (F * invOnePlusPr + Pr * dFdPr);
+    }
+    o.Kf = Mt * (invOnePlusPr * F * K0);
+    return o;
+}
+
+// ------------------------------------------------------------------------
 // right-hand side: FastChemistryModel::derivatives (FastChemistryModel.C:194-273
 // for mode 1, 340-417 for mode 2) over OptReaction::dNdtByV
 // (ReactionRate.C:732-1503).  YT is clamped (Y >= 0) in place.
@@ -474,7 +570,20 @@ __device__ __noinline__ void rhs_eval(const Grp<G>& g, const DevMech& M, const S
     g.sync();
     const PFactor pf = pressure_factors(Tc);
     const double logP = M.nPlog ? log(p) : 0.0;
-    for (int r = g.rank; r < M.nr; r += G) {
+    // Fall-off reactions fill one contiguous block [foBegin, foBegin + nFo) of
+    // the packed order and run in a loop of their own, so that the main loop
+    // carries no call to falloff_rate.
+    auto finish = [&](const int r, const RxnInfo& x, const double Kf) {
+        double Kr = 0;
+        if (x.rev) Kr = Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
+        double CF = s.C[x.sl[0]];
+        for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
+        double CR = s.C[x.sr[0]];
+        for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
+        s.q[r] = Kf * CF - Kr * CR;
+    };
+    for (int j = g.rank; j < M.nr - M.nFo; j += G) {
+        const int r = j < M.foBegin ? j : j + M.nFo;
         const RxnInfo x = load_rx(M.rx + r);
         double Kf;
         if (x.kind == FCS_RXN_PLOG) {
@@ -486,13 +595,12 @@ __device__ __noinline__ void rhs_eval(const Grp<G>& g, const DevMech& M, const S
             Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
         }
         if (x.tb >= 0) Kf *= s.Mtb[x.tb];
-        double Kr = 0;
-        if (x.rev) Kr = Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
-        double CF = s.C[x.sl[0]];
-        for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
-        double CR = s.C[x.sr[0]];
-        for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
-        s.q[r] = Kf * CF - Kr * CR;
+        finish(r, x, Kf);
+    }
+    for (int r = M.foBegin + g.rank; r < M.foBegin + M.nFo; r += G) {
+        const RxnInfo x = load_rx(M.rx + r);
+        const double K0 = x.tind ? x.A : x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
+        finish(r, x, falloff_rate(M, x, K0, 0.0, s.Mtb[x.tb], Tc, logT, invT, false).Kf);
     }
     g.sync();
     double cpm = 0, dtd = 0;
@@ -560,18 +668,10 @@ __device__ __noinline__ double tc_eval(const Grp<G>& g, const DevMech& M, const 
     const double PByRT = kPstd / (kRu * Tc);
     const double logP = M.nPlog ? log(p) : 0.0;
     double sw = 0, sw2 = 0;
-    for (int r = g.rank; r < M.nr; r += G) {
-        const RxnInfo x = load_rx(M.rx + r);
-        double Kf;
-        if (x.kind == FCS_RXN_PLOG) {
-            double dk;
-            Kf = plog_rate(M, x.plog, p, logP, logT, invT, &dk);
-        } else if (x.tind) {
-            Kf = x.A;
-        } else {
-            Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
-        }
-        if (x.tb >= 0) Kf *= s.Mtb[x.tb];
+    // Fall-off reactions fill one contiguous block [foBegin, foBegin + nFo) of
+    // the packed order and run in a loop of their own, so that the main loop
+    // carries no call to falloff_rate.
+    auto finish = [&](const int r, const RxnInfo& x, const double Kf) {
         double Kr = 0;
         if (x.rev) {
             double Kp = 1.0;
@@ -588,6 +688,26 @@ __device__ __noinline__ double tc_eval(const Grp<G>& g, const DevMech& M, const 
         const double wf = x.nr * (Kf * CF), wr = x.nl * (Kr * CR);
         sw += wf + wr;
         sw2 = fma(wf, wf, fma(wr, wr, sw2));
+    };
+    for (int j = g.rank; j < M.nr - M.nFo; j += G) {
+        const int r = j < M.foBegin ? j : j + M.nFo;
+        const RxnInfo x = load_rx(M.rx + r);
+        double Kf;
+        if (x.kind == FCS_RXN_PLOG) {
+            double dk;
+            Kf = plog_rate(M, x.plog, p, logP, logT, invT, &dk);
+        } else if (x.tind) {
+            Kf = x.A;
+        } else {
+            Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
+        }
+        if (x.tb >= 0) Kf *= s.Mtb[x.tb];
+        finish(r, x, Kf);
+    }
+    for (int r = M.foBegin + g.rank; r < M.foBegin + M.nFo; r += G) {
+        const RxnInfo x = load_rx(M.rx + r);
+        const double K0 = x.tind ? x.A : x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
+        finish(r, x, falloff_rate(M, x, K0, 0.0, s.Mtb[x.tb], Tc, logT, invT, false).Kf);
     }
     gsum2(g, sw, sw2, s.red);
     return sw2 == 0 ? 1e300 : sw / sw2 * sumc;
@@ -621,7 +741,20 @@ __device__ __noinline__ double rates_eval(const Grp<G>& g, const DevMech& M, con
     g.sync();
     const PFactor pf = pressure_factors(Tc);
     const double logP = M.nPlog ? log(p) : 0.0;
-    for (int r = g.rank; r < M.nr; r += G) {
+    // Fall-off reactions fill one contiguous block [foBegin, foBegin + nFo) of
+    // the packed order and run in a loop of their own, so that the main loop
+    // carries no call to falloff_rate.
+    auto finish = [&](const int r, const RxnInfo& x, const double Kf) {
+        double Kr = 0;
+        if (x.rev) Kr = Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
+        double CF = s.C[x.sl[0]];
+        for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
+        double CR = s.C[x.sr[0]];
+        for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
+        s.q[r] = Kf * CF - Kr * CR;
+    };
+    for (int j = g.rank; j < M.nr - M.nFo; j += G) {
+        const int r = j < M.foBegin ? j : j + M.nFo;
         const RxnInfo x = load_rx(M.rx + r);
         double Kf;
         if (x.kind == FCS_RXN_PLOG) {
@@ -633,13 +766,12 @@ __device__ __noinline__ double rates_eval(const Grp<G>& g, const DevMech& M, con
             Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
         }
         if (x.tb >= 0) Kf *= s.Mtb[x.tb];
-        double Kr = 0;
-        if (x.rev) Kr = Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
-        double CF = s.C[x.sl[0]];
-        for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
-        double CR = s.C[x.sr[0]];
-        for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
-        s.q[r] = Kf * CF - Kr * CR;
+        finish(r, x, Kf);
+    }
+    for (int r = M.foBegin + g.rank; r < M.foBegin + M.nFo; r += G) {
+        const RxnInfo x = load_rx(M.rx + r);
+        const double K0 = x.tind ? x.A : x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
+        finish(r, x, falloff_rate(M, x, K0, 0.0, s.Mtb[x.tb], Tc, logT, invT, false).Kf);
     }
     g.sync();
     double qd = 0;
@@ -724,24 +856,11 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
     // per-reaction rate constants, their temperature derivatives and q
     const PFactor pf = pressure_factors(Tc);
     const double logP = M.nPlog ? log(p) : 0.0;
-    for (int r = g.rank; r < M.nr; r += G) {
-        const RxnInfo x = load_rx(M.rx + r);
-        double Kf, dKfdT;
-        if (x.kind == FCS_RXN_PLOG) {
-            Kf = plog_rate(M, x.plog, p, logP, logT, invT, &dKfdT);
-        } else if (x.tind) {
-            Kf = x.A; dKfdT = 0;
-        } else {
-            Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
-            dKfdT = Kf * (fma(x.Ta, invT, x.beta) * invT);
-        }
-        double dKfdC = 0;
-        if (x.tb >= 0) {
-            const double Mt = s.Mtb[x.tb];
-            dKfdC = Kf;
-            Kf *= Mt;
-            dKfdT *= Mt;
-        }
+    // Fall-off reactions fill one contiguous block [foBegin, foBegin + nFo) of
+    // the packed order and run in a loop of their own, so that the main loop
+    // carries no call to falloff_rate.
+    auto finish = [&](const int r, const RxnInfo& x, const double Kf, const double dKfdT,
+                      const double dKfdC) {
         double Kr = 0, dKrdT = 0, invKc = 0;
         if (x.rev) {
             invKc = inv_equilibrium_kc(x, s.B, s.Binv, pf);
@@ -764,6 +883,37 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
         s.dqdT[r] = dKfdT * CF - dKrdT * CR;
         // third-body weight w = dKf/dM CF - dKr/dM CR, dKr/dM = dKf/dM / Kc
         if (x.tb >= 0) s.tbF[x.tb] = dKfdC * CF - (dKfdC * invKc) * CR;
+    };
+    for (int j = g.rank; j < M.nr - M.nFo; j += G) {
+        const int r = j < M.foBegin ? j : j + M.nFo;
+        const RxnInfo x = load_rx(M.rx + r);
+        double Kf, dKfdT;
+        if (x.kind == FCS_RXN_PLOG) {
+            Kf = plog_rate(M, x.plog, p, logP, logT, invT, &dKfdT);
+        } else if (x.tind) {
+            Kf = x.A; dKfdT = 0;
+        } else {
+            Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
+            dKfdT = Kf * (fma(x.Ta, invT, x.beta) * invT);
+        }
+        double dKfdC = 0;
+        if (x.tb >= 0) {
+            const double Mt = s.Mtb[x.tb];
+            dKfdC = Kf;
+            Kf *= Mt;
+            dKfdT *= Mt;
+        }
+        finish(r, x, Kf, dKfdT, dKfdC);
+    }
+    for (int r = M.foBegin + g.rank; r < M.foBegin + M.nFo; r += G) {
+        const RxnInfo x = load_rx(M.rx + r);
+        double K0 = x.A, dK0dT = 0;
+        if (!x.tind) {
+            K0 = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
+            dK0dT = K0 * (fma(x.Ta, invT, x.beta) * invT);
+        }
+        const FalloffK k = falloff_rate(M, x, K0, dK0dT, s.Mtb[x.tb], Tc, logT, invT, true);
+        finish(r, x, k.Kf, k.dKfdT, k.dKfdC);
     }
     for (int idx = g.rank; idx < ns * ld; idx += G) J[idx] = MT(0);
     g.sync();

@@ -35,13 +35,15 @@ struct RxnInfo {            // 64 bytes
     int32_t plog;           // PLOG index or -1
     int32_t dnu;            // nr - nl
     int32_t tind;           // temperature independent (beta == 0 and Ta == 0)
-    int32_t pad[2];
+    int32_t fo;             // fall-off index (kInf and F parameters in DevMech::fo) or -1
+    int32_t pad;
 };
 static_assert(sizeof(RxnInfo) == 64, "RxnInfo must stay 64 bytes");
 
 struct DevMech {
     int ns, n, nr;
     int nTB, nPlog;
+    int foBegin, nFo;       // fall-off reactions: one contiguous block of the packed order
     double TlowMin, ThighMax, TcommonMin, TcommonMax;
     const double* W;        // [ns]
     const double* invW;     // [ns]
@@ -57,6 +59,7 @@ struct DevMech {
     int nTbInc;             // third-body incidences (species row, third-body row, side)
     const int* tbInc;       // (row << 16) | (tb << 1) | (1 if product else 0), reaction order
     const double* hf;       // [ns] formation enthalpy at 298.15 K, J/kg (for Qdot)
+    const double* fo;       // [n fall-off][8]: kInf A, beta, Ta; Troe alpha, T*, T**, T*** / SRI a, b, c, d, e
 };
 
 // Per-cell options the kernels need (copied by value into kernel params).

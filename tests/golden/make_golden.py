@@ -33,6 +33,8 @@ CASES = [
     ("ignition_10s", 64, "OptRosenbrock23"),
     ("counterflow_53s", 8, "OptRodas23"),
     ("counterflow_53s", 4, "OptRosenbrock23"),
+    ("falloff_16s", 64, "OptRodas34"),
+    ("falloff_16s", 32, "OptSeulex"),
 ]
 
 
@@ -66,6 +68,7 @@ TC = [
     ("ignition_10s", 64),
     ("counterflow_53s", 64),
     ("uneven_111s", 64),
+    ("falloff_16s", 64),
 ]
 
 

@@ -63,7 +63,7 @@ def test_exp_against_cuda(built):
 
 
 @pytest.mark.parametrize("wname,n", [("ignition_10s", 64), ("counterflow_53s", 32), ("uneven_111s", 16),
-                                     ("large_200s", 4)])
+                                     ("large_200s", 4), ("falloff_16s", 64)])
 def test_rhs_and_jacobian_match_oracle(built, wname, n):
     import oracle
     w, mech, flat, c = _setup(wname, n)
@@ -94,7 +94,8 @@ def test_fast_jacobian_matches_oracle(built):
 GOLDEN_CASES = ["ignition_10s_OptRodas34", "ignition_10s_OptRosenbrock34", "ignition_10s_OptSeulex",
                 "counterflow_53s_OptRodas34", "counterflow_53s_OptRosenbrock34", "counterflow_53s_OptSeulex",
                 "ignition_10s_OptRodas23", "ignition_10s_OptRosenbrock23",
-                "counterflow_53s_OptRodas23", "counterflow_53s_OptRosenbrock23"]
+                "counterflow_53s_OptRodas23", "counterflow_53s_OptRosenbrock23",
+                "falloff_16s_OptRodas34", "falloff_16s_OptSeulex"]
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
@@ -299,7 +300,7 @@ def test_queue_order_and_graph_replay_do_not_change_results(built):
             assert s[k] == s0[k], k
 
 
-@pytest.mark.parametrize("wname", ["ignition_10s", "counterflow_53s", "uneven_111s"])
+@pytest.mark.parametrize("wname", ["ignition_10s", "counterflow_53s", "uneven_111s", "falloff_16s"])
 def test_tc_matches_reference_golden(built, wname):
     """fcs_tc against FastChemistryModel::tc() of the reference
     (tests/golden/tc.npz); differences are summation order and exp rounding."""

@@ -17,8 +17,16 @@ def test_generator_sizes_and_balance(name):
         assert 1 <= len(r.lhs) <= 3 and 1 <= len(r.rhs) <= 3
         # atom conservation by construction
         assert np.array_equal(m.composition[r.lhs].sum(0), m.composition[r.rhs].sum(0))
-        assert 6.0 <= np.log10(r.A * 1000.0 ** r.beta) <= 14.0 + 1e-9
-        assert -2 <= r.beta <= 3 and 0 <= r.Ta <= 30000
+        if r.kinf is not None:
+            # fall-off: kInf in the generic ranges, k0 (per unit of M) 10-1000x above it at 1000 K
+            A, beta, Ta = r.kinf
+            lg = np.log10(r.A * 1000.0 ** r.beta) - np.log10(A * 1000.0 ** beta)
+            assert 1.0 - 1e-9 <= lg <= 3.0 + 1e-9
+            assert beta - 1.5 <= r.beta <= beta and 0 <= r.Ta <= 0.5 * Ta
+        else:
+            A, beta, Ta = r.A, r.beta, r.Ta
+        assert 6.0 <= np.log10(A * 1000.0 ** beta) <= 14.0 + 1e-9
+        assert -2 <= beta <= 3 and 0 <= Ta <= 30000
     # cp(T) of every fit stays in [25, 60] J/mol/K over 300..3000 K (small fit error allowed)
     T = np.linspace(300, 3000, 28)
     for i in range(m.n_species):

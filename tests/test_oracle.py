@@ -19,7 +19,8 @@ def _golden(name):
 CASES = ["ignition_10s_OptRodas34", "ignition_10s_OptRosenbrock34", "ignition_10s_OptSeulex",
          "counterflow_53s_OptRodas34", "counterflow_53s_OptRosenbrock34", "counterflow_53s_OptSeulex",
          "ignition_10s_OptRodas23", "ignition_10s_OptRosenbrock23",
-         "counterflow_53s_OptRodas23", "counterflow_53s_OptRosenbrock23"]
+         "counterflow_53s_OptRodas23", "counterflow_53s_OptRosenbrock23",
+         "falloff_16s_OptRodas34", "falloff_16s_OptSeulex"]
 
 
 def _setup(case):
@@ -60,7 +61,7 @@ def test_port_matches_reference_integration(case, port_built):
         assert abs(out["counters"]["jacobians"] - int(g["jacobians"])) <= max(2, 0.002 * int(g["jacobians"]))
 
 
-@pytest.mark.parametrize("case", ["ignition_10s_OptRodas34", "counterflow_53s_OptRodas34"])
+@pytest.mark.parametrize("case", ["ignition_10s_OptRodas34", "counterflow_53s_OptRodas34", "falloff_16s_OptRodas34"])
 def test_port_matches_reference_rhs_and_jacobian(case, port_built):
     import oracle
     w, flat, solver, g, cells = _setup(case)
@@ -120,7 +121,7 @@ def test_port_against_compiled_reference_directly(port_built):
     np.testing.assert_allclose(r1["Y"], r0["Y"], atol=1e-9)
 
 
-@pytest.mark.parametrize("wname", ["ignition_10s", "counterflow_53s", "uneven_111s"])
+@pytest.mark.parametrize("wname", ["ignition_10s", "counterflow_53s", "uneven_111s", "falloff_16s"])
 def test_port_tc_matches_reference_golden(wname, port_built):
     """FastChemistryModel::tc() of the reference (tests/golden/tc.npz)."""
     import oracle
