@@ -137,23 +137,26 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
                    !d->rhs_species || !d->arrhenius))
         return set_err(ctx, FCS_ERR_INVALID, "missing reaction arrays");
     std::vector<int> order;
-    // type blocks: T-independent Arrhenius, Arrhenius, third body, fall-off
+    // type blocks: T-independent Arrhenius, Arrhenius, non-equilibrium,
+    // non-equilibrium third body (OptReaction.C:610-700), third body, fall-off
     // (Lindemann, Troe, SRI: OptReaction.C:746-917), PLOG
-    for (int pass = 0; pass < 7; pass++) {
+    static const int kBlocks[] = {FCS_RXN_ARRHENIUS, FCS_RXN_ARRHENIUS, FCS_RXN_NONEQ, FCS_RXN_NONEQ_THIRD_BODY,
+                                  FCS_RXN_THIRD_BODY, FCS_RXN_LINDEMANN_FALLOFF, FCS_RXN_TROE_FALLOFF,
+                                  FCS_RXN_SRI_FALLOFF, FCS_RXN_PLOG};
+    for (int pass = 0; pass < 9; pass++) {
         for (int r = 0; r < nr; r++) {
             const int t = d->type[r];
+            if (t != kBlocks[pass]) continue;
             const bool tind = d->arrhenius[3 * r + 1] == 0 && d->arrhenius[3 * r + 2] == 0;
-            if ((pass == 0 && t == FCS_RXN_ARRHENIUS && tind) || (pass == 1 && t == FCS_RXN_ARRHENIUS && !tind) ||
-                (pass == 2 && t == FCS_RXN_THIRD_BODY) || (pass == 3 && t == FCS_RXN_LINDEMANN_FALLOFF) ||
-                (pass == 4 && t == FCS_RXN_TROE_FALLOFF) || (pass == 5 && t == FCS_RXN_SRI_FALLOFF) ||
-                (pass == 6 && t == FCS_RXN_PLOG))
-                order.push_back(r);
+            if (t == FCS_RXN_ARRHENIUS && tind != (pass == 0)) continue;
+            order.push_back(r);
         }
     }
     if ((int)order.size() != nr)
         return set_err(ctx, FCS_ERR_UNSUPPORTED,
                        "reaction types other than (ir)reversible Arrhenius, ThirdBodyArrhenius, "
-                       "ArrheniusLindemann/Troe/SRIFallOff and ArrheniusPLOG are not supported by the GPU path");
+                       "ArrheniusLindemann/Troe/SRIFallOff, ArrheniusPLOG and nonEquilibriumReversible"
+                       "(ThirdBody)Arrhenius are not supported by the GPU path");
     std::vector<double> W(ns), invW(ns), Tc(ns), coef(16 * (size_t)ns, 0.0), hf(ns);
     double TlowMin = 1e10, ThighMax = 1, TcMin = 1e10, TcMax = 0;
     for (int i = 0; i < ns; i++) {
@@ -210,13 +213,15 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
             x.sr[q] = int16_t(sp);
             inc[sp].push_back((k << 1) | 1);
         }
-        x.rev = d->reversible[r] ? 1 : 0;
+        const bool noneq = d->type[r] == FCS_RXN_NONEQ || d->type[r] == FCS_RXN_NONEQ_THIRD_BODY;
+        x.rev = noneq ? 2 : d->reversible[r] ? 1 : 0;
         x.kind = int8_t(d->type[r]);
         x.dnu = x.nr - x.nl;
         x.tind = (x.beta == 0 && x.Ta == 0) ? 1 : 0;
         x.tb = -1;
         x.plog = -1;
         x.fo = -1;
+        x.nq = -1;
         const bool falloff = d->type[r] >= FCS_RXN_LINDEMANN_FALLOFF && d->type[r] <= FCS_RXN_SRI_FALLOFF;
         if (falloff) {
             if (!d->arrhenius2) return set_err(ctx, FCS_ERR_INVALID, "fall-off reaction without kInf (arrhenius2)");
@@ -226,7 +231,15 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
             for (int q = 0; q < 3; q++) fo.push_back(d->arrhenius2[3 * (size_t)r + q]);
             for (int q = 0; q < 5; q++) fo.push_back(d->falloff_params ? d->falloff_params[5 * (size_t)r + q] : 0.0);
         }
-        if (d->type[r] == FCS_RXN_THIRD_BODY || falloff) {
+        if (noneq) {
+            // the reverse rate's own Arrhenius (OptReaction.C:628-630, 663-665)
+            if (!d->arrhenius2)
+                return set_err(ctx, FCS_ERR_INVALID, "non-equilibrium reaction without a reverse rate (arrhenius2)");
+            x.nq = (int)(fo.size() / 8);
+            for (int q = 0; q < 3; q++) fo.push_back(d->arrhenius2[3 * (size_t)r + q]);
+            for (int q = 0; q < 5; q++) fo.push_back(0.0);
+        }
+        if (d->type[r] == FCS_RXN_THIRD_BODY || d->type[r] == FCS_RXN_NONEQ_THIRD_BODY || falloff) {
             if (!d->efficiencies) return set_err(ctx, FCS_ERR_INVALID, "third-body reaction without efficiencies");
             for (int s = 0; s < ns; s++) eff.push_back(d->efficiencies[(size_t)r * ns + s]);
             x.tb = nTB++;
@@ -280,12 +293,14 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
     M.plogTa = ctx->dPlogTa.p; M.incOff = ctx->dIncOff.p; M.inc = ctx->dInc.p; M.hf = ctx->dHf.p;
     M.nTbInc = nTbInc; M.tbInc = ctx->dTbInc.p;
     M.fo = ctx->dFo.p;
-    M.foBegin = 0;
-    M.nFo = 0;
+    // the special block: first to last non-equilibrium or fall-off reaction
+    // (third-body reactions between them included)
+    M.spBegin = 0;
+    M.nSp = 0;
     for (int k = 0; k < nr; k++)
-        if (rx[k].fo >= 0) {
-            if (M.nFo == 0) M.foBegin = k;
-            M.nFo++;
+        if (rx[k].fo >= 0 || rx[k].nq >= 0) {
+            if (M.nSp == 0) M.spBegin = k;
+            M.nSp = k + 1 - M.spBegin;
         }
     ctx->loaded = true;
     ctx->tuned.clear();

@@ -524,6 +524,51 @@ static __device__ __noinline__ FalloffK falloff_rate(const DevMech& M, const Rxn
     return o;
 }
 
+// Rates of one reaction of the special block: fall-off, non-equilibrium (the
+// reverse rate its own Arrhenius, ReactionRate.C:362-367, 540-544) or
+// third-body; Kf and Kr include M, and with deriv the temperature derivatives
+// and dKf/dM, dKr/dM (Jacobian.C:401-422).
+struct SpecialK { double Kf, dKfdT, dKfdC, Kr, dKrdT, dKrdC; };
+
+static __device__ __forceinline__ SpecialK special_rates(const DevMech& M, const RxnInfo& x, const double* Mtb,
+                                                      double Tc, double logT, double invT, bool deriv) {
+    SpecialK o{0, 0, 0, 0, 0, 0};
+    double K0 = x.A, dK0dT = 0;
+    if (!x.tind) {
+        K0 = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
+        dK0dT = K0 * (fma(x.Ta, invT, x.beta) * invT);
+    }
+    const double Mt = x.tb >= 0 ? Mtb[x.tb] : 1.0;
+    if (x.fo >= 0) {
+        const FalloffK k = falloff_rate(M, x, K0, dK0dT, Mt, Tc, logT, invT, deriv);
+        o.Kf = k.Kf;
+        o.dKfdT = k.dKfdT;
+        o.dKfdC = k.dKfdC;
+    } else if (x.tb >= 0) {
+        o.dKfdC = K0;
+        o.Kf = K0 * Mt;
+        o.dKfdT = dK0dT * Mt;
+    } else {
+        o.Kf = K0;
+        o.dKfdT = dK0dT;
+    }
+    if (x.nq >= 0) {
+        const double* f = M.fo + (size_t)x.nq * 8;
+        const double Ar = __ldg(f), br = __ldg(f + 1), Tar = __ldg(f + 2);
+        const double Kr = Ar * fast_exp(fma(br, logT, -(Tar * invT)));
+        const double dKrdT = Kr * (fma(Tar, invT, br) * invT);
+        if (x.tb >= 0) {
+            o.dKrdC = Kr;
+            o.Kr = Kr * Mt;
+            o.dKrdT = dKrdT * Mt;
+        } else {
+            o.Kr = Kr;
+            o.dKrdT = dKrdT;
+        }
+    }
+    return o;
+}
+
 // ------------------------------------------------------------------------
 // right-hand side: FastChemistryModel::derivatives (FastChemistryModel.C:194-273
 // for mode 1, 340-417 for mode 2) over OptReaction::dNdtByV
@@ -570,20 +615,19 @@ __device__ __noinline__ void rhs_eval(const Grp<G>& g, const DevMech& M, const S
     g.sync();
     const PFactor pf = pressure_factors(Tc);
     const double logP = M.nPlog ? log(p) : 0.0;
-    // Fall-off reactions fill one contiguous block [foBegin, foBegin + nFo) of
-    // the packed order and run in a loop of their own, so that the main loop
-    // carries no call to falloff_rate.
-    auto finish = [&](const int r, const RxnInfo& x, const double Kf) {
-        double Kr = 0;
-        if (x.rev) Kr = Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
+    // The special block [spBegin, spBegin + nSp) of the packed order (first
+    // non-equilibrium to last fall-off reaction) runs in a loop of its own, so
+    // that the main loop carries neither the fall-off call nor a second
+    // Arrhenius.
+    auto finish = [&](const int r, const RxnInfo& x, const double Kf, const double Kr) {
         double CF = s.C[x.sl[0]];
         for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
         double CR = s.C[x.sr[0]];
         for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
         s.q[r] = Kf * CF - Kr * CR;
     };
-    for (int j = g.rank; j < M.nr - M.nFo; j += G) {
-        const int r = j < M.foBegin ? j : j + M.nFo;
+    for (int j = g.rank; j < M.nr - M.nSp; j += G) {
+        const int r = j < M.spBegin ? j : j + M.nSp;
         const RxnInfo x = load_rx(M.rx + r);
         double Kf;
         if (x.kind == FCS_RXN_PLOG) {
@@ -595,12 +639,16 @@ __device__ __noinline__ void rhs_eval(const Grp<G>& g, const DevMech& M, const S
             Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
         }
         if (x.tb >= 0) Kf *= s.Mtb[x.tb];
-        finish(r, x, Kf);
+        double Kr = 0;
+        if (x.rev) Kr = Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
+        finish(r, x, Kf, Kr);
     }
-    for (int r = M.foBegin + g.rank; r < M.foBegin + M.nFo; r += G) {
+    for (int r = M.spBegin + g.rank; r < M.spBegin + M.nSp; r += G) {
         const RxnInfo x = load_rx(M.rx + r);
-        const double K0 = x.tind ? x.A : x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
-        finish(r, x, falloff_rate(M, x, K0, 0.0, s.Mtb[x.tb], Tc, logT, invT, false).Kf);
+        const SpecialK k = special_rates(M, x, s.Mtb, Tc, logT, invT, false);
+        double Kr = k.Kr;  // non-equilibrium: its own reverse rate
+        if (x.rev == 1) Kr = k.Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
+        finish(r, x, k.Kf, Kr);
     }
     g.sync();
     double cpm = 0, dtd = 0;
@@ -668,12 +716,15 @@ __device__ __noinline__ double tc_eval(const Grp<G>& g, const DevMech& M, const 
     const double PByRT = kPstd / (kRu * Tc);
     const double logP = M.nPlog ? log(p) : 0.0;
     double sw = 0, sw2 = 0;
-    // Fall-off reactions fill one contiguous block [foBegin, foBegin + nFo) of
-    // the packed order and run in a loop of their own, so that the main loop
-    // carries no call to falloff_rate.
+    // The special block [spBegin, spBegin + nSp) of the packed order (first
+    // non-equilibrium to last fall-off reaction) runs in a loop of its own, so
+    // that the main loop carries neither the fall-off call nor a second
+    // Arrhenius.
+    // Tc.C:578-600: the reverse rate only through Kc; a non-equilibrium
+    // reaction counts with its forward rate alone
     auto finish = [&](const int r, const RxnInfo& x, const double Kf) {
         double Kr = 0;
-        if (x.rev) {
+        if (x.rev == 1) {
             double Kp = 1.0;
             for (int q = 0; q < x.nl; q++) Kp = Kp / s.B[x.sl[q]];
             for (int q = 0; q < x.nr; q++) Kp = Kp * s.B[x.sr[q]];
@@ -689,8 +740,8 @@ __device__ __noinline__ double tc_eval(const Grp<G>& g, const DevMech& M, const 
         sw += wf + wr;
         sw2 = fma(wf, wf, fma(wr, wr, sw2));
     };
-    for (int j = g.rank; j < M.nr - M.nFo; j += G) {
-        const int r = j < M.foBegin ? j : j + M.nFo;
+    for (int j = g.rank; j < M.nr - M.nSp; j += G) {
+        const int r = j < M.spBegin ? j : j + M.nSp;
         const RxnInfo x = load_rx(M.rx + r);
         double Kf;
         if (x.kind == FCS_RXN_PLOG) {
@@ -704,10 +755,9 @@ __device__ __noinline__ double tc_eval(const Grp<G>& g, const DevMech& M, const 
         if (x.tb >= 0) Kf *= s.Mtb[x.tb];
         finish(r, x, Kf);
     }
-    for (int r = M.foBegin + g.rank; r < M.foBegin + M.nFo; r += G) {
+    for (int r = M.spBegin + g.rank; r < M.spBegin + M.nSp; r += G) {
         const RxnInfo x = load_rx(M.rx + r);
-        const double K0 = x.tind ? x.A : x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
-        finish(r, x, falloff_rate(M, x, K0, 0.0, s.Mtb[x.tb], Tc, logT, invT, false).Kf);
+        finish(r, x, special_rates(M, x, s.Mtb, Tc, logT, invT, false).Kf);
     }
     gsum2(g, sw, sw2, s.red);
     return sw2 == 0 ? 1e300 : sw / sw2 * sumc;
@@ -741,20 +791,19 @@ __device__ __noinline__ double rates_eval(const Grp<G>& g, const DevMech& M, con
     g.sync();
     const PFactor pf = pressure_factors(Tc);
     const double logP = M.nPlog ? log(p) : 0.0;
-    // Fall-off reactions fill one contiguous block [foBegin, foBegin + nFo) of
-    // the packed order and run in a loop of their own, so that the main loop
-    // carries no call to falloff_rate.
-    auto finish = [&](const int r, const RxnInfo& x, const double Kf) {
-        double Kr = 0;
-        if (x.rev) Kr = Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
+    // The special block [spBegin, spBegin + nSp) of the packed order (first
+    // non-equilibrium to last fall-off reaction) runs in a loop of its own, so
+    // that the main loop carries neither the fall-off call nor a second
+    // Arrhenius.
+    auto finish = [&](const int r, const RxnInfo& x, const double Kf, const double Kr) {
         double CF = s.C[x.sl[0]];
         for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
         double CR = s.C[x.sr[0]];
         for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
         s.q[r] = Kf * CF - Kr * CR;
     };
-    for (int j = g.rank; j < M.nr - M.nFo; j += G) {
-        const int r = j < M.foBegin ? j : j + M.nFo;
+    for (int j = g.rank; j < M.nr - M.nSp; j += G) {
+        const int r = j < M.spBegin ? j : j + M.nSp;
         const RxnInfo x = load_rx(M.rx + r);
         double Kf;
         if (x.kind == FCS_RXN_PLOG) {
@@ -766,12 +815,16 @@ __device__ __noinline__ double rates_eval(const Grp<G>& g, const DevMech& M, con
             Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
         }
         if (x.tb >= 0) Kf *= s.Mtb[x.tb];
-        finish(r, x, Kf);
+        double Kr = 0;
+        if (x.rev) Kr = Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
+        finish(r, x, Kf, Kr);
     }
-    for (int r = M.foBegin + g.rank; r < M.foBegin + M.nFo; r += G) {
+    for (int r = M.spBegin + g.rank; r < M.spBegin + M.nSp; r += G) {
         const RxnInfo x = load_rx(M.rx + r);
-        const double K0 = x.tind ? x.A : x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
-        finish(r, x, falloff_rate(M, x, K0, 0.0, s.Mtb[x.tb], Tc, logT, invT, false).Kf);
+        const SpecialK k = special_rates(M, x, s.Mtb, Tc, logT, invT, false);
+        double Kr = k.Kr;  // non-equilibrium: its own reverse rate
+        if (x.rev == 1) Kr = k.Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
+        finish(r, x, k.Kf, Kr);
     }
     g.sync();
     double qd = 0;
@@ -856,23 +909,26 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
     // per-reaction rate constants, their temperature derivatives and q
     const PFactor pf = pressure_factors(Tc);
     const double logP = M.nPlog ? log(p) : 0.0;
-    // Fall-off reactions fill one contiguous block [foBegin, foBegin + nFo) of
-    // the packed order and run in a loop of their own, so that the main loop
-    // carries no call to falloff_rate.
-    auto finish = [&](const int r, const RxnInfo& x, const double Kf, const double dKfdT,
-                      const double dKfdC) {
-        double Kr = 0, dKrdT = 0, invKc = 0;
-        if (x.rev) {
-            invKc = inv_equilibrium_kc(x, s.B, s.Binv, pf);
-            double sv = s.dBdT[x.sr[0]];
-            for (int q = 1; q < x.nr; q++) sv += s.dBdT[x.sr[q]];
-            double sl = s.dBdT[x.sl[0]];
-            for (int q = 1; q < x.nl; q++) sl += s.dBdT[x.sl[q]];
-            const double dKcdTByKc = (sv - sl) - x.dnu * invT;
-            Kr = Kf * invKc;
-            // the Kc term of dKr/dT is dropped when Kc sits on its clamp (JacobianFunctionI.H:246-249)
-            dKrdT = dKfdT * invKc - (invKc < kInvKcClamp ? Kr * dKcdTByKc : 0.0);
-        }
+    // The special block [spBegin, spBegin + nSp) of the packed order (first
+    // non-equilibrium to last fall-off reaction) runs in a loop of its own, so
+    // that the main loop carries neither the fall-off call nor a second
+    // Arrhenius.
+    // Kr, dKr/dT and dKr/dM through Kc (JF* reversible branch)
+    auto through_kc = [&](const RxnInfo& x, const double Kf, const double dKfdT, const double dKfdC,
+                          double& Kr, double& dKrdT, double& dKrdC) {
+        const double invKc = inv_equilibrium_kc(x, s.B, s.Binv, pf);
+        double sv = s.dBdT[x.sr[0]];
+        for (int q = 1; q < x.nr; q++) sv += s.dBdT[x.sr[q]];
+        double sl = s.dBdT[x.sl[0]];
+        for (int q = 1; q < x.nl; q++) sl += s.dBdT[x.sl[q]];
+        const double dKcdTByKc = (sv - sl) - x.dnu * invT;
+        Kr = Kf * invKc;
+        // the Kc term of dKr/dT is dropped when Kc sits on its clamp (JacobianFunctionI.H:246-249)
+        dKrdT = dKfdT * invKc - (invKc < kInvKcClamp ? Kr * dKcdTByKc : 0.0);
+        dKrdC = dKfdC * invKc;
+    };
+    auto finish = [&](const int r, const RxnInfo& x, const double Kf, const double dKfdT, const double dKfdC,
+                      const double Kr, const double dKrdT, const double dKrdC) {
         double CF = s.C[x.sl[0]];
         for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
         double CR = s.C[x.sr[0]];
@@ -881,11 +937,11 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
         s.Kr[r] = Kr;
         s.q[r] = Kf * CF - Kr * CR;
         s.dqdT[r] = dKfdT * CF - dKrdT * CR;
-        // third-body weight w = dKf/dM CF - dKr/dM CR, dKr/dM = dKf/dM / Kc
-        if (x.tb >= 0) s.tbF[x.tb] = dKfdC * CF - (dKfdC * invKc) * CR;
+        // third-body weight w = dKf/dM CF - dKr/dM CR
+        if (x.tb >= 0) s.tbF[x.tb] = dKfdC * CF - dKrdC * CR;
     };
-    for (int j = g.rank; j < M.nr - M.nFo; j += G) {
-        const int r = j < M.foBegin ? j : j + M.nFo;
+    for (int j = g.rank; j < M.nr - M.nSp; j += G) {
+        const int r = j < M.spBegin ? j : j + M.nSp;
         const RxnInfo x = load_rx(M.rx + r);
         double Kf, dKfdT;
         if (x.kind == FCS_RXN_PLOG) {
@@ -903,17 +959,16 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
             Kf *= Mt;
             dKfdT *= Mt;
         }
-        finish(r, x, Kf, dKfdT, dKfdC);
+        double Kr = 0, dKrdT = 0, dKrdC = 0;
+        if (x.rev) through_kc(x, Kf, dKfdT, dKfdC, Kr, dKrdT, dKrdC);
+        finish(r, x, Kf, dKfdT, dKfdC, Kr, dKrdT, dKrdC);
     }
-    for (int r = M.foBegin + g.rank; r < M.foBegin + M.nFo; r += G) {
+    for (int r = M.spBegin + g.rank; r < M.spBegin + M.nSp; r += G) {
         const RxnInfo x = load_rx(M.rx + r);
-        double K0 = x.A, dK0dT = 0;
-        if (!x.tind) {
-            K0 = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
-            dK0dT = K0 * (fma(x.Ta, invT, x.beta) * invT);
-        }
-        const FalloffK k = falloff_rate(M, x, K0, dK0dT, s.Mtb[x.tb], Tc, logT, invT, true);
-        finish(r, x, k.Kf, k.dKfdT, k.dKfdC);
+        SpecialK k = special_rates(M, x, s.Mtb, Tc, logT, invT, true);
+        // non-equilibrium: the reverse Arrhenius (JacobianFunctionI.H:129-130, Jacobian.C:412-422)
+        if (x.rev == 1) through_kc(x, k.Kf, k.dKfdT, k.dKfdC, k.Kr, k.dKrdT, k.dKrdC);
+        finish(r, x, k.Kf, k.dKfdT, k.dKfdC, k.Kr, k.dKrdT, k.dKrdC);
     }
     for (int idx = g.rank; idx < ns * ld; idx += G) J[idx] = MT(0);
     g.sync();

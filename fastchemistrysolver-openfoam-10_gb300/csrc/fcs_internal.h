@@ -29,21 +29,22 @@ struct RxnInfo {            // 64 bytes
     int16_t sl[kMaxSide];   // reactant species (repeated by stoichiometry)
     int16_t sr[kMaxSide];   // product species
     int8_t nl, nr;          // counts
-    int8_t rev;             // 1 reversible
+    int8_t rev;             // 1 reversible (Kr = Kf / Kc), 2 non-equilibrium (Kr its own Arrhenius)
     int8_t kind;            // FCS_RXN_*
     int32_t tb;             // third-body row or -1
     int32_t plog;           // PLOG index or -1
     int32_t dnu;            // nr - nl
     int32_t tind;           // temperature independent (beta == 0 and Ta == 0)
     int32_t fo;             // fall-off index (kInf and F parameters in DevMech::fo) or -1
-    int32_t pad;
+    int32_t nq;             // non-equilibrium reverse-rate index (A, beta, Ta in DevMech::fo) or -1
 };
 static_assert(sizeof(RxnInfo) == 64, "RxnInfo must stay 64 bytes");
 
 struct DevMech {
     int ns, n, nr;
     int nTB, nPlog;
-    int foBegin, nFo;       // fall-off reactions: one contiguous block of the packed order
+    int spBegin, nSp;       // special block of the packed order: first to last non-equilibrium or
+                            // fall-off reaction
     double TlowMin, ThighMax, TcommonMin, TcommonMax;
     const double* W;        // [ns]
     const double* invW;     // [ns]
@@ -59,7 +60,8 @@ struct DevMech {
     int nTbInc;             // third-body incidences (species row, third-body row, side)
     const int* tbInc;       // (row << 16) | (tb << 1) | (1 if product else 0), reaction order
     const double* hf;       // [ns] formation enthalpy at 298.15 K, J/kg (for Qdot)
-    const double* fo;       // [n fall-off][8]: kInf A, beta, Ta; Troe alpha, T*, T**, T*** / SRI a, b, c, d, e
+    const double* fo;       // [n fall-off + n non-equilibrium][8]: kInf A, beta, Ta; Troe alpha, T*, T**,
+                            // T*** / SRI a, b, c, d, e -- or the reverse A, beta, Ta of a non-equilibrium reaction
 };
 
 // Per-cell options the kernels need (copied by value into kernel params).

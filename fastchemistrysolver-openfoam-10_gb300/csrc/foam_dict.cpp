@@ -1,6 +1,7 @@
 // foam_dict.cpp -- reader for the OpenFOAM dictionaries the plugin consumes:
 // the `reactions` dictionary (with `reversibleArrheniusPLOG` /
-// `ArrheniusData`), the species thermo entries (`specie{molWeight}`,
+// `ArrheniusData`, fall-off k0 / kInf / F / thirdBodyEfficiencies and
+// non-equilibrium forward / reverse entries), the species thermo entries (`specie{molWeight}`,
 // `thermodynamics{Tlow,Thigh,Tcommon,highCpCoeffs,lowCpCoeffs}`) and the
 // `chemistryProperties` keys.  It builds an fcs_mechanism_desc the way
 // OptReaction::readInfo (src/Reaction/OptReaction.C:348-1339) and
@@ -275,19 +276,24 @@ extern "C" fcs_status fcs_load_mechanism_foam(fcs_ctx* ctx, const char* reaction
         std::string tname, eq;
         if (!as_word(r->find("type"), tname)) return FCS_ERR_PARSE;
         if (!as_word(r->find("reaction"), eq)) return FCS_ERR_PARSE;
-        int reversible;
+        int reversible = 1;
         std::string base;
-        if (tname.rfind("irreversible", 0) == 0) { reversible = 0; base = tname.substr(12); }
+        int kind = -1;
+        if (tname == "nonEquilibriumReversibleArrhenius") kind = FCS_RXN_NONEQ;
+        else if (tname == "nonEquilibriumReversibleThirdBodyArrhenius") kind = FCS_RXN_NONEQ_THIRD_BODY;
+        else if (tname.rfind("irreversible", 0) == 0) { reversible = 0; base = tname.substr(12); }
         else if (tname.rfind("reversible", 0) == 0) { reversible = 1; base = tname.substr(10); }
-        else return FCS_ERR_UNSUPPORTED;  // nonEquilibrium* and unknown types
-        int kind;
-        if (base == "Arrhenius") kind = FCS_RXN_ARRHENIUS;
-        else if (base == "ThirdBodyArrhenius") kind = FCS_RXN_THIRD_BODY;
-        else if (base == "ArrheniusPLOG") kind = FCS_RXN_PLOG;
-        else if (base == "ArrheniusLindemannFallOff") kind = FCS_RXN_LINDEMANN_FALLOFF;
-        else if (base == "ArrheniusTroeFallOff") kind = FCS_RXN_TROE_FALLOFF;
-        else if (base == "ArrheniusSRIFallOff") kind = FCS_RXN_SRI_FALLOFF;
-        else return FCS_ERR_UNSUPPORTED;
+        else return FCS_ERR_UNSUPPORTED;  // chemically activated, Landau-Teller and other unknown types
+        if (kind < 0) {
+            if (base == "Arrhenius") kind = FCS_RXN_ARRHENIUS;
+            else if (base == "ThirdBodyArrhenius") kind = FCS_RXN_THIRD_BODY;
+            else if (base == "ArrheniusPLOG") kind = FCS_RXN_PLOG;
+            else if (base == "ArrheniusLindemannFallOff") kind = FCS_RXN_LINDEMANN_FALLOFF;
+            else if (base == "ArrheniusTroeFallOff") kind = FCS_RXN_TROE_FALLOFF;
+            else if (base == "ArrheniusSRIFallOff") kind = FCS_RXN_SRI_FALLOFF;
+            else return FCS_ERR_UNSUPPORTED;
+        }
+        const bool noneq = kind == FCS_RXN_NONEQ || kind == FCS_RXN_NONEQ_THIRD_BODY;
         // reaction string (readReactionInfo, OptReaction.C:29-173): terms
         // separated by '+', sides by '=', integer coefficients expanded
         std::istringstream iss(eq);
@@ -320,15 +326,19 @@ extern "C" fcs_status fcs_load_mechanism_foam(fcs_ctx* ctx, const char* reaction
         ro.push_back((int32_t)rs.size());
         type.push_back(kind);
         rev.push_back(reversible);
+        const bool falloff = kind >= FCS_RXN_LINDEMANN_FALLOFF && kind <= FCS_RXN_SRI_FALLOFF;
         double A = 0, beta = 0, Ta = 0;
-        const Node* k0 = (kind >= FCS_RXN_LINDEMANN_FALLOFF) ? r->find("k0") : r;
+        // forward rate: the reaction dict, k0 (fall-off) or forward (non-equilibrium,
+        // OptReaction.C:620-631)
+        const Node* k0 = falloff ? r->find("k0") : noneq ? r->find("forward") : r;
         if (!k0 || !as_double(k0->find("A"), A) || !as_double(k0->find("beta"), beta) ||
             !as_double(k0->find("Ta"), Ta))
             return FCS_ERR_PARSE;
         arr.push_back(A); arr.push_back(beta); arr.push_back(Ta);
         double kA = 0, kb = 0, kt = 0;
-        if (kind >= FCS_RXN_LINDEMANN_FALLOFF) {
-            const Node* ki = r->find("kInf");
+        if (falloff || noneq) {
+            // second Arrhenius: kInf, or the reverse rate of a non-equilibrium reaction
+            const Node* ki = r->find(falloff ? "kInf" : "reverse");
             if (!ki || !as_double(ki->find("A"), kA) || !as_double(ki->find("beta"), kb) ||
                 !as_double(ki->find("Ta"), kt))
                 return FCS_ERR_PARSE;
@@ -337,7 +347,10 @@ extern "C" fcs_status fcs_load_mechanism_foam(fcs_ctx* ctx, const char* reaction
         std::vector<double> row(ns, 1.0);
         const Node* cnode = nullptr;
         if (kind == FCS_RXN_THIRD_BODY) cnode = r->find("coeffs");
-        else if (kind >= FCS_RXN_LINDEMANN_FALLOFF) {
+        // the reference takes both directions' coefficients from the forward
+        // dictionary (OptReaction.C:668-686)
+        else if (kind == FCS_RXN_NONEQ_THIRD_BODY) cnode = k0->find("coeffs");
+        else if (falloff) {
             const Node* tb = r->find("thirdBodyEfficiencies");
             if (tb) cnode = tb->find("coeffs");
         }

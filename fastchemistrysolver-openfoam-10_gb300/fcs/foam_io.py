@@ -1,5 +1,6 @@
 """Writers for the OpenFOAM dictionaries the plugin reads: ``reactions`` (with
-``species`` list, and ``ArrheniusData`` for PLOG reactions), the species
+``species`` list, ``ArrheniusData`` for PLOG reactions, k0 / kInf / F for
+fall-off and forward / reverse for non-equilibrium reactions), the species
 thermo entries (``specie{molWeight}``, ``thermodynamics{...}``) and a
 ``chemistryProperties`` file.  The layout follows the reference tutorials
 (e.g. tutorial/Ignition0D/*/constant/{reactions,speciesThermo}).
@@ -8,30 +9,63 @@ from __future__ import annotations
 
 import os
 
-from .mechanism import ARRHENIUS, PLOG, THIRD_BODY, Mechanism
+from typing import List
+
+from .mechanism import (FALLOFF_KINDS, NONEQ_KINDS, NONEQ_THIRD_BODY, PLOG, SRI_FALLOFF, THIRD_BODY, TROE_FALLOFF,
+                        TYPE_NAMES, Mechanism)
 
 
 def _num(x: float) -> str:
     return repr(float(x))
 
 
+def _coeffs(m: Mechanism, eff, indent: str) -> List[str]:
+    return ([f"{indent}coeffs          {m.n_species}", "("] +
+            [f"({m.species[i]} {_num(e)})" for i, e in enumerate(eff)] + [")", ";"])
+
+
+def _arrhenius_block(name: str, abt, indent: str, extra: List[str] = ()) -> List[str]:
+    A, beta, Ta = abt
+    return ([f"{indent}{name}", f"{indent}{{",
+             f"{indent}    A               {_num(A)};",
+             f"{indent}    beta            {_num(beta)};",
+             f"{indent}    Ta              {_num(Ta)};"] + list(extra) + [f"{indent}}}"])
+
+
 def write_reactions(m: Mechanism, path: str) -> None:
+    """Every kind in the layout of the reference's tutorial mechanisms:
+    k0 / kInf / F / thirdBodyEfficiencies for fall-off, forward / reverse
+    sub-dictionaries (with the coefficient list in both) for the
+    non-equilibrium kinds."""
     lines = [f"species {m.n_species} ( {' '.join(m.species)} );", "", "reactions", "{"]
     for k, r in enumerate(m.reactions):
-        prefix = "reversible" if r.reversible else "irreversible"
-        kind = {ARRHENIUS: "Arrhenius", THIRD_BODY: "ThirdBodyArrhenius", PLOG: "ArrheniusPLOG"}[r.kind]
+        if r.kind in NONEQ_KINDS:
+            tname = TYPE_NAMES[r.kind]
+        else:
+            tname = ("reversible" if r.reversible else "irreversible") + TYPE_NAMES[r.kind]
         lines += [f"    un-named-reaction-{k}", "    {",
-                  f"        type            {prefix}{kind};",
-                  f'        reaction        "{m.reaction_string(r)}";',
-                  f"        A               {_num(r.A)};",
-                  f"        beta            {_num(r.beta)};",
-                  f"        Ta              {_num(r.Ta)};"]
+                  f"        type            {tname};",
+                  f'        reaction        "{m.reaction_string(r)}";']
+        if r.kind in FALLOFF_KINDS:
+            lines += _arrhenius_block("k0", (r.A, r.beta, r.Ta), "        ")
+            lines += _arrhenius_block("kInf", r.kinf, "        ")
+            names = {TROE_FALLOFF: ("alpha", "Ts", "Tss", "Tsss"), SRI_FALLOFF: ("a", "b", "c", "d", "e")}
+            lines += ["        F", "        {"]
+            for nm, v in zip(names.get(r.kind, ()), r.falloff or ()):
+                lines.append(f"            {nm:<16}{_num(v)};")
+            lines += ["        }", "        thirdBodyEfficiencies", "        {"]
+            lines += _coeffs(m, r.efficiencies, "            ")
+            lines.append("        }")
+        elif r.kind in NONEQ_KINDS:
+            tb = _coeffs(m, r.efficiencies, "            ") if r.kind == NONEQ_THIRD_BODY else []
+            lines += _arrhenius_block("forward", (r.A, r.beta, r.Ta), "        ", tb)
+            lines += _arrhenius_block("reverse", r.reverse, "        ", tb)
+        else:
+            lines += [f"        A               {_num(r.A)};",
+                      f"        beta            {_num(r.beta)};",
+                      f"        Ta              {_num(r.Ta)};"]
         if r.kind == THIRD_BODY:
-            lines.append(f"        coeffs          {m.n_species}")
-            lines.append("(")
-            lines += [f"({m.species[i]} {_num(e)})" for i, e in enumerate(r.efficiencies)]
-            lines.append(")")
-            lines.append(";")
+            lines += _coeffs(m, r.efficiencies, "        ")
         if r.kind == PLOG:
             lines.append("        ArrheniusData")
             lines.append("        (")

@@ -42,7 +42,14 @@ PLOG = 2
 LINDEMANN_FALLOFF = 3
 TROE_FALLOFF = 4
 SRI_FALLOFF = 5
+NONEQ = 6
+NONEQ_THIRD_BODY = 7
 
+FALLOFF_KINDS = (LINDEMANN_FALLOFF, TROE_FALLOFF, SRI_FALLOFF)
+NONEQ_KINDS = (NONEQ, NONEQ_THIRD_BODY)
+
+# OpenFOAM type names; the (ir)reversible prefix is added by the writer except
+# for the non-equilibrium kinds, whose names carry it
 TYPE_NAMES = {
     ARRHENIUS: "Arrhenius",
     THIRD_BODY: "ThirdBodyArrhenius",
@@ -50,6 +57,8 @@ TYPE_NAMES = {
     LINDEMANN_FALLOFF: "ArrheniusLindemannFallOff",
     TROE_FALLOFF: "ArrheniusTroeFallOff",
     SRI_FALLOFF: "ArrheniusSRIFallOff",
+    NONEQ: "nonEquilibriumReversibleArrhenius",
+    NONEQ_THIRD_BODY: "nonEquilibriumReversibleThirdBodyArrhenius",
 }
 
 ELEMENTS = ("H", "C", "O", "N")
@@ -70,6 +79,7 @@ class Reaction:
     plog: Optional[np.ndarray] = None              # [rows, 4] (p, A, beta, Ta)
     kinf: Optional[Sequence[float]] = None         # (A, beta, Ta) for falloff
     falloff: Optional[Sequence[float]] = None      # Troe (alpha, Ts, Tss, Tsss) / SRI (a,b,c,d,e)
+    reverse: Optional[Sequence[float]] = None      # (A, beta, Ta) reverse rate of non-equilibrium kinds
 
 
 @dataclasses.dataclass
@@ -122,6 +132,9 @@ class Mechanism:
                 h.update(np.asarray(r.efficiencies, dtype=np.float64).tobytes())
             if r.plog is not None:
                 h.update(np.asarray(r.plog, dtype=np.float64).tobytes())
+            for extra in (r.kinf, r.falloff, r.reverse):
+                if extra is not None:
+                    h.update(np.asarray(extra, dtype=np.float64).tobytes())
         return h.hexdigest()[:16]
 
 
@@ -302,7 +315,7 @@ def synthetic_mechanism(n_species: int, n_reactions: int, n_third_body: int,
                         n_plog: int, seed: int, n_elements: int = 3,
                         max_count: int = 3, plog_points: int = 5,
                         plog_p_range=(1e4, 1e8), hf_range_kJ=(-100.0, 100.0),
-                        name: Optional[str] = None, n_falloff=(0, 0, 0)) -> Mechanism:
+                        name: Optional[str] = None, n_falloff=(0, 0, 0), n_noneq=(0, 0)) -> Mechanism:
     """Build one seeded synthetic mechanism (all reactions reversible).
 
     The reactions are emitted in a shuffled *file* order so that the type
@@ -382,6 +395,31 @@ def synthetic_mechanism(n_species: int, n_reactions: int, n_third_body: int,
                 fo = None
             reactions.append(Reaction(kind, True, lr[0], lr[1], A0 * T_REF_ARRHENIUS ** (beta - beta0), beta0, Ta0,
                                       efficiencies=eff, kinf=(A, beta, Ta), falloff=fo))
+    # non-equilibrium reversible (plain and third-body): the reverse rate is
+    # its own Arrhenius, fitted to Kf/Kc at 1000 K and 2000 K with the forward
+    # beta and then moved off equilibrium by a factor 10^U(-0.5, 0.5)
+    for kind, count in zip(NONEQ_KINDS, n_noneq):
+        for _ in range(count):
+            lr = builder.exchange() if kind == NONEQ else (builder.recombination() or builder.exchange())
+            if lr is None:
+                lr = builder.exchange()
+            if lr is None:
+                raise RuntimeError("could not close a non-equilibrium template; change the seed")
+            lr = orient(lr)
+            A, beta, Ta = _arrhenius(rng)
+            g = []
+            for T in (1000.0, 2000.0):
+                B = np.array([_minus_G_over_RT(high[i], T) for i in range(n_species)])
+                dnu = len(lr[1]) - len(lr[0])
+                lnKc = B[lr[1]].sum() - B[lr[0]].sum() + dnu * math.log(1e5 / (8314.47 * T))
+                g.append(math.log(A) - Ta / T - lnKc)   # ln(Kf / Kc) - beta ln T
+            Ta_r = (g[1] - g[0]) / (1.0 / 1000.0 - 1.0 / 2000.0)
+            if Ta_r < 0:
+                Ta_r = 0.0
+            lnA_r = g[0] + Ta_r / 1000.0 + rng.uniform(-0.5, 0.5) * math.log(10.0)
+            eff = rng.uniform(0.5, 5.0, size=n_species) if kind == NONEQ_THIRD_BODY else None
+            reactions.append(Reaction(kind, True, lr[0], lr[1], A, beta, Ta, efficiencies=eff,
+                                      reverse=(math.exp(lnA_r), beta, Ta_r)))
     while len(reactions) < n_reactions:
         r = rng.random()
         lr = builder.exchange() if r < 0.8 else builder.recombination()
@@ -452,6 +490,8 @@ def flatten(m: Mechanism) -> FlatMechanism:
     for i, r in enumerate(m.reactions):
         if r.kinf is not None:
             arr2[3 * i:3 * i + 3] = r.kinf
+        if r.reverse is not None:
+            arr2[3 * i:3 * i + 3] = r.reverse
         if r.efficiencies is not None:
             eff[i * ns:(i + 1) * ns] = r.efficiencies
         if r.falloff is not None:

@@ -22,6 +22,10 @@ Workloads (all seeds fixed):
   Lindemann, Troe and SRI fall-off), 512 cells, T ~ U[900, 1800] K,
   p log-uniform on [1e4, 1e7] Pa, Y ~ Dirichlet(0.5), dt = 1e-5 s: the parity
   case of the fall-off kinds (no benchmark field uses them).
+* ``noneq_14s`` -- 14 species / 40 reactions (6 non-equilibrium reversible,
+  3 non-equilibrium third-body, 2 third-body, 1 PLOG, 1 Lindemann, 1 Troe),
+  512 cells drawn like ``falloff_16s``: the parity case of the
+  non-equilibrium kinds.
 * ``large_200s`` -- 200 species / 1,500 reactions (60 PLOG, 40 third-body),
   1,048,576 cells, T ~ U[600, 2400] K, p ~ U[1e5, 4e6] Pa, Y ~ Dirichlet(0.2),
   dt = 1e-5 s.
@@ -98,6 +102,11 @@ WORKLOADS = {
         "falloff_16s",
         dict(n_species=16, n_reactions=48, n_third_body=3, n_plog=2, seed=1616, n_falloff=(3, 3, 3)),
         n_cells=512, dt=1e-5, cell_seed=16),
+    "noneq_14s": Workload(
+        "noneq_14s",
+        dict(n_species=14, n_reactions=40, n_third_body=2, n_plog=1, seed=1414, n_falloff=(1, 1, 0),
+             n_noneq=(6, 3)),
+        n_cells=512, dt=1e-5, cell_seed=14),
     "large_200s": Workload(
         "large_200s",
         dict(n_species=200, n_reactions=1500, n_third_body=40, n_plog=60, seed=2000),
@@ -138,7 +147,7 @@ def cells_for(w: Workload, mech: Mechanism, n: Optional[int] = None,
                               rng.uniform(1200.0, 2200.0, n_full)))
         p = rng.uniform(1e5, 1e6, n_full)
         Y = rng.dirichlet(np.full(ns, 0.3), size=n_full).T
-    elif w.name == "falloff_16s":
+    elif w.name in ("falloff_16s", "noneq_14s"):
         T = rng.uniform(900.0, 1800.0, n_full)
         p = 10.0 ** rng.uniform(4.0, 7.0, n_full)
         Y = rng.dirichlet(np.full(ns, 0.5), size=n_full).T

@@ -73,7 +73,10 @@ enum {
     FCS_RXN_PLOG = 2,                /* (ir)reversibleArrheniusPLOG                */
     FCS_RXN_LINDEMANN_FALLOFF = 3,   /* (ir)reversibleArrheniusLindemannFallOff    */
     FCS_RXN_TROE_FALLOFF = 4,        /* (ir)reversibleArrheniusTroeFallOff         */
-    FCS_RXN_SRI_FALLOFF = 5          /* (ir)reversibleArrheniusSRIFallOff          */
+    FCS_RXN_SRI_FALLOFF = 5,         /* (ir)reversibleArrheniusSRIFallOff          */
+    FCS_RXN_NONEQ = 6,               /* nonEquilibriumReversibleArrhenius: forward
+                                        and reverse rates both Arrhenius (no Kc)  */
+    FCS_RXN_NONEQ_THIRD_BODY = 7     /* nonEquilibriumReversibleThirdBodyArrhenius */
 };
 
 enum { FCS_SOLVER_RODAS34 = 0, FCS_SOLVER_ROSENBROCK34 = 1, FCS_SOLVER_SEULEX = 2,
@@ -106,8 +109,9 @@ enum {
 /*
  * Mechanism in OpenFOAM file order.  The library reorders the reactions into
  * the type blocks of OptReaction::readInfo (OptReaction.C:348-1339): constant
- * Arrhenius (beta == 0 and Ta == 0) first, then the other Arrhenius, then
- * third-body, fall-off, then PLOG.  Stoichiometric coefficients are expanded
+ * Arrhenius (beta == 0 and Ta == 0) first, then the other Arrhenius,
+ * non-equilibrium, non-equilibrium third-body, third-body, fall-off, then
+ * PLOG.  Stoichiometric coefficients are expanded
  * into repeated species entries exactly as readReactionInfo does
  * (OptReaction.C:29-173).  The host keeps ownership; the library copies.
  */
@@ -126,10 +130,17 @@ typedef struct fcs_mechanism_desc {
     const int32_t* lhs_species;  /* reactant species, repeated by coefficient   */
     const int32_t* rhs_offset;   /* [R+1]                                       */
     const int32_t* rhs_species;  /* product species, repeated by coefficient    */
-    const double* arrhenius;     /* [R*3] A, beta, Ta (k0 for fall-off)         */
-    const double* arrhenius2;    /* [R*3] kInf A, beta, Ta for fall-off; may be NULL */
+    const double* arrhenius;     /* [R*3] A, beta, Ta (k0 for fall-off, the
+                                    forward rate for non-equilibrium)           */
+    const double* arrhenius2;    /* [R*3] kInf A, beta, Ta for fall-off, the
+                                    reverse rate for non-equilibrium; may be NULL
+                                    when neither kind occurs                    */
     const double* efficiencies;  /* [R*Ns] third-body efficiencies (row used for
-                                    third-body and fall-off reactions); may be NULL */
+                                    third-body, fall-off and non-equilibrium
+                                    third-body reactions; the latter use it for
+                                    both directions, as the reference reads the
+                                    reverse list from the forward dictionary,
+                                    OptReaction.C:678); may be NULL */
     const double* falloff_params;/* [R*5] Troe alpha,Ts,Tss,Tsss / SRI a,b,c,d,e */
     const int32_t* plog_offset;  /* [R+1] rows of plog_table per reaction       */
     const double* plog_table;    /* [rows*4] p, A, beta, Ta (ArrheniusData)     */

@@ -33,6 +33,10 @@
 #define PIV_EPS 2.2204460492503131e-16
 #define SMALL 1.0e-15
 #define VGREAT 1.0e300
+#define IS_FALLOFF(k) ((k) >= FCS_RXN_LINDEMANN_FALLOFF && (k) <= FCS_RXN_SRI_FALLOFF)
+#define IS_NONEQ(k) ((k) == FCS_RXN_NONEQ || (k) == FCS_RXN_NONEQ_THIRD_BODY)
+/* kinds that take a third-body row: M = E C */
+#define HAS_TB(k) ((k) == FCS_RXN_THIRD_BODY || (k) == FCS_RXN_NONEQ_THIRD_BODY || IS_FALLOFF(k))
 
 struct orc_mech {
     int ns, n, nr;
@@ -42,9 +46,9 @@ struct orc_mech {
     /* per reaction, reference order */
     int *kind, *rev, *fileIdx, *lOff, *lSp, *rOff, *rSp, *tbRow, *plogIdx, *dnu;
     double *A, *beta, *Ta;
-    double *A2, *beta2, *Ta2;    /* kInf of fall-off reactions (per reaction) */
+    double *A2, *beta2, *Ta2;    /* per reaction: kInf of fall-off, reverse rate of non-equilibrium */
     double *fo;                  /* [nr][5] Troe (alpha, Ts, Tss, Tsss) / SRI (a, b, c, d, e) */
-    double *eff;                 /* [nTB][ns]: third-body rows, then fall-off rows */
+    double *eff;                 /* [nTB][ns]: non-equilibrium third-body, third-body, then fall-off rows */
     int *pOff;                   /* [nPlog+1] */
     double *pP, *pLogP, *pLogA, *pBeta, *pTa;
     int maxSp;
@@ -71,17 +75,22 @@ void orc_mech_destroy(orc_mech* m)
 }
 
 /* Type-block order of OptReaction::readInfo (OptReaction.C:448-1175):
- * temperature-independent Arrhenius, other Arrhenius, (non-equilibrium),
- * third-body, fall-off (Lindemann, then Troe, then SRI: OptReaction.C:746-917),
- * (chemically activated), PLOG; file order inside each block.  Fall-off
- * reactions take third-body rows after the third-body reactions' (Itbr[2]). */
+ * temperature-independent Arrhenius, other Arrhenius, non-equilibrium,
+ * non-equilibrium third-body (OptReaction.C:610-700), third-body, fall-off
+ * (Lindemann, then Troe, then SRI: OptReaction.C:746-917), (chemically
+ * activated), PLOG; file order inside each block.  Third-body rows follow the
+ * same order (Itbr[0..3]); rev is 2 for non-equilibrium reactions
+ * (isIrreversible = 2, OptReaction.C:619, 654), whose reverse rate is their
+ * own Arrhenius.  The reference builds the reverse third-body row of a
+ * non-equilibrium reaction from the forward coefficients (OptReaction.C:678),
+ * so one row serves both directions. */
 orc_mech* orc_mech_create(const fcs_mechanism_desc* d, int32_t* status)
 {
     *status = FCS_OK;
     const int ns = d->n_species, nr = d->n_reactions;
     for (int r = 0; r < nr; r++) {
         int t = d->type[r];
-        if (t < FCS_RXN_ARRHENIUS || t > FCS_RXN_SRI_FALLOFF) {
+        if (t < FCS_RXN_ARRHENIUS || t > FCS_RXN_NONEQ_THIRD_BODY) {
             *status = FCS_ERR_UNSUPPORTED;
             return NULL;
         }
@@ -106,18 +115,20 @@ orc_mech* orc_mech_create(const fcs_mechanism_desc* d, int32_t* status)
     }
     int* order = (int*)malloc(sizeof(int) * (nr > 0 ? nr : 1));
     int k = 0;
-    for (int pass = 0; pass < 7; pass++) {
+    for (int pass = 0; pass < 9; pass++) {
         for (int r = 0; r < nr; r++) {
             int t = d->type[r];
             double beta = d->arrhenius[3 * r + 1], Ta = d->arrhenius[3 * r + 2];
             int tind = (beta == 0 && Ta == 0);
             if ((pass == 0 && t == FCS_RXN_ARRHENIUS && tind) ||
                 (pass == 1 && t == FCS_RXN_ARRHENIUS && !tind) ||
-                (pass == 2 && t == FCS_RXN_THIRD_BODY) ||
-                (pass == 3 && t == FCS_RXN_LINDEMANN_FALLOFF) ||
-                (pass == 4 && t == FCS_RXN_TROE_FALLOFF) ||
-                (pass == 5 && t == FCS_RXN_SRI_FALLOFF) ||
-                (pass == 6 && t == FCS_RXN_PLOG))
+                (pass == 2 && t == FCS_RXN_NONEQ) ||
+                (pass == 3 && t == FCS_RXN_NONEQ_THIRD_BODY) ||
+                (pass == 4 && t == FCS_RXN_THIRD_BODY) ||
+                (pass == 5 && t == FCS_RXN_LINDEMANN_FALLOFF) ||
+                (pass == 6 && t == FCS_RXN_TROE_FALLOFF) ||
+                (pass == 7 && t == FCS_RXN_SRI_FALLOFF) ||
+                (pass == 8 && t == FCS_RXN_PLOG))
                 order[k++] = r;
         }
     }
@@ -132,8 +143,8 @@ orc_mech* orc_mech_create(const fcs_mechanism_desc* d, int32_t* status)
     ALLOC_I(m->lSp, nl_tot); ALLOC_I(m->rSp, nr_tot);
     int nTB = 0, nPlog = 0, plogRows = 0;
     for (int r = 0; r < nr; r++) {
-        if (d->type[r] == FCS_RXN_THIRD_BODY || d->type[r] >= FCS_RXN_LINDEMANN_FALLOFF) nTB++;
-        if (d->type[r] >= FCS_RXN_LINDEMANN_FALLOFF) m->nFO++;
+        if (HAS_TB(d->type[r])) nTB++;
+        if (IS_FALLOFF(d->type[r])) m->nFO++;
         if (d->type[r] == FCS_RXN_PLOG) { nPlog++; plogRows += d->plog_offset[r + 1] - d->plog_offset[r]; }
     }
     m->nTB = nTB; m->nPlog = nPlog;
@@ -147,7 +158,7 @@ orc_mech* orc_mech_create(const fcs_mechanism_desc* d, int32_t* status)
         int r = order[i];
         m->fileIdx[i] = r;
         m->kind[i] = d->type[r];
-        m->rev[i] = d->reversible[r] ? 1 : 0;
+        m->rev[i] = IS_NONEQ(d->type[r]) ? 2 : d->reversible[r] ? 1 : 0;
         m->A[i] = d->arrhenius[3 * r + 0];
         m->beta[i] = d->arrhenius[3 * r + 1];
         m->Ta[i] = d->arrhenius[3 * r + 2];
@@ -162,16 +173,17 @@ orc_mech* orc_mech_create(const fcs_mechanism_desc* d, int32_t* status)
         m->dnu[i] = nrr - nlr;
         m->tbRow[i] = -1;
         m->plogIdx[i] = -1;
-        if (m->kind[i] == FCS_RXN_THIRD_BODY || m->kind[i] >= FCS_RXN_LINDEMANN_FALLOFF) {
+        if (HAS_TB(m->kind[i])) {
             for (int s = 0; s < ns; s++) m->eff[tb * ns + s] = d->efficiencies[(size_t)r * ns + s];
             m->tbRow[i] = tb++;
         }
-        if (m->kind[i] >= FCS_RXN_LINDEMANN_FALLOFF) {
+        if (IS_FALLOFF(m->kind[i]) || IS_NONEQ(m->kind[i])) {
             m->A2[i] = d->arrhenius2[3 * r + 0];
             m->beta2[i] = d->arrhenius2[3 * r + 1];
             m->Ta2[i] = d->arrhenius2[3 * r + 2];
-            for (int q = 0; q < 5; q++) m->fo[(size_t)i * 5 + q] = d->falloff_params[(size_t)r * 5 + q];
         }
+        if (IS_FALLOFF(m->kind[i]))
+            for (int q = 0; q < 5; q++) m->fo[(size_t)i * 5 + q] = d->falloff_params[(size_t)r * 5 + q];
         if (m->kind[i] == FCS_RXN_PLOG) {
             m->plogIdx[i] = pl;
             m->pOff[pl] = prow;
@@ -205,7 +217,7 @@ typedef struct {
     int n;
     double *C, *B, *dBdT, *Cp, *Ha, *dCpdT, *rhoMvj, *WiByrhoM;
     double *Kf, *dKfdT, *M, *Kplog, *dKplog;
-    double *Kinf, *dKinfdT;      /* kInf of fall-off reactions */
+    double *Kinf, *dKinfdT;      /* second Arrhenius: kInf (fall-off), reverse rate (non-equilibrium) */
     double *Jc, *Jy, *a;       /* N*N each */
     double *vec[16];           /* N each */
     int *piv;
@@ -344,8 +356,10 @@ static void arrhenius_rates(const orc_mech* m, ws_t* w, double logT, double invT
         const double k = m->A[i] * exp(fma(m->beta[i], logT, -(m->Ta[i] * invT)));
         w->Kf[i] = k;
         if (withDeriv) w->dKfdT[i] = k * (fma(m->Ta[i], invT, m->beta[i]) * invT);
-        if (m->kind[i] >= FCS_RXN_LINDEMANN_FALLOFF) {
-            /* kInf sits at Ikf[7] + (i - Ikf[4]) in the reference's Kf_ (OptReaction.C:768-772) */
+        if (IS_FALLOFF(m->kind[i]) || IS_NONEQ(m->kind[i])) {
+            /* the second Arrhenius: kInf sits at Ikf[7] + (i - Ikf[4]) in the
+             * reference's Kf_ (OptReaction.C:768-772), a non-equilibrium
+             * reverse rate at Ikf[9] + (i - Ikf[1]) (OptReaction.C:628-630) */
             const double ki = m->A2[i] * exp(fma(m->beta2[i], logT, -(m->Ta2[i] * invT)));
             w->Kinf[i] = ki;
             if (withDeriv) w->dKinfdT[i] = ki * (fma(m->Ta2[i], invT, m->beta2[i]) * invT);
@@ -524,8 +538,8 @@ static void dNdtByV(const orc_mech* m, ws_t* w, double p, double T, double* omeg
     arrhenius_rates(m, w, logT, invT, 0);
     third_body(m, w);
     for (int i = 0; i < m->nr; i++) {
-        if (m->kind[i] == FCS_RXN_THIRD_BODY) w->Kf[i] *= w->M[m->tbRow[i]];
-        else if (m->kind[i] >= FCS_RXN_LINDEMANN_FALLOFF) w->Kf[i] = falloff_rate(m, w, i, Tc, invT, NULL, NULL);
+        if (m->kind[i] == FCS_RXN_THIRD_BODY || m->kind[i] == FCS_RXN_NONEQ_THIRD_BODY) w->Kf[i] *= w->M[m->tbRow[i]];
+        else if (IS_FALLOFF(m->kind[i])) w->Kf[i] = falloff_rate(m, w, i, Tc, invT, NULL, NULL);
     }
     if (m->nPlog) plog_rates(m, w, p, logT, invT, 0);
     memset(omega, 0, sizeof(double) * ns);
@@ -535,7 +549,12 @@ static void dNdtByV(const orc_mech* m, ws_t* w, double p, double T, double* omeg
         const int* R = &m->rSp[m->rOff[i]];
         const int nl = m->lOff[i + 1] - m->lOff[i], nr = m->rOff[i + 1] - m->rOff[i];
         double Kr = 0;
-        if (m->rev[i]) Kr = Kf / equilibrium(m, i, w->B, PByRT);
+        if (m->rev[i] == 1) Kr = Kf / equilibrium(m, i, w->B, PByRT);
+        else if (m->rev[i] == 2) {
+            /* ReactionRate.C:362-367, 540-544: the reverse Arrhenius, times M for third-body */
+            Kr = w->Kinf[i];
+            if (m->tbRow[i] >= 0) Kr *= w->M[m->tbRow[i]];
+        }
         const double q = Kf * prod_sp(L, nl, w->C) - Kr * prod_sp(R, nr, w->C);
         for (int s = 0; s < nl; s++) omega[L[s]] -= q;
         for (int s = 0; s < nr; s++) omega[R[s]] += q;
@@ -624,7 +643,7 @@ static void jacobian(const orc_mech* m, ws_t* w, const orc_options* o, double p,
         int tb = m->tbRow[i];
         if (m->kind[i] == FCS_RXN_PLOG) { Kf = w->Kplog[m->plogIdx[i]]; dKfdT = w->dKplog[m->plogIdx[i]]; }
         else { Kf = w->Kf[i]; dKfdT = w->dKfdT[i]; }
-        if (m->kind[i] >= FCS_RXN_LINDEMANN_FALLOFF) {
+        if (IS_FALLOFF(m->kind[i])) {
             Kf = falloff_rate(m, w, i, Tc, invT, &dKfdT, &dKfdC);
         } else if (tb >= 0) {
             /* Jacobian.C:401-420: dKf/dM = Kf(before M), Kf *= M, dKf/dT *= M */
@@ -635,8 +654,8 @@ static void jacobian(const orc_mech* m, ws_t* w, const orc_options* o, double p,
         const int* L = &m->lSp[m->lOff[i]];
         const int* R = &m->rSp[m->rOff[i]];
         const int nl = m->lOff[i + 1] - m->lOff[i], nr = m->rOff[i + 1] - m->rOff[i];
-        double Kr = 0, dKrdT = 0, invKc = 0;
-        if (m->rev[i]) {
+        double Kr = 0, dKrdT = 0, invKc = 0, dKrdC = 0;
+        if (m->rev[i] == 1) {
             /* JF* reversible branch, e.g. JacobianFunctionI.H:1127-1297 */
             const double Kc = equilibrium(m, i, w->B, PByRT);
             const double clamp = (nl > 3 || nr > 3) ? KC_CLAMP_G : KC_CLAMP;
@@ -649,6 +668,20 @@ static void jacobian(const orc_mech* m, ws_t* w, const orc_options* o, double p,
             invKc = 1.0 / Kc;
             Kr = Kf * invKc;
             dKrdT = dKfdT * invKc - (Kc > clamp ? Kr * dKcdTByKc : 0);
+            dKrdC = dKfdC * invKc;
+        } else if (m->rev[i] == 2) {
+            /* non-equilibrium overloads of JF*, e.g. JacobianFunctionI.H:100-230:
+             * Kr and dKr/dT of the reverse Arrhenius (Jacobian.C:412-422 scale
+             * them by M and keep the raw rate as dKr/dM) */
+            Kr = w->Kinf[i];
+            dKrdT = w->dKinfdT[i];
+            if (tb >= 0) {
+                dKrdC = Kr;
+                Kr *= w->M[tb];
+                dKrdT *= w->M[tb];
+            }
+        }
+        if (m->rev[i]) {
             for (int pp = 0; pp < nr; pp++) {
                 double d = 1.0;
                 for (int q = 0; q < nr; q++) if (q != pp) d *= C[R[q]];
@@ -675,7 +708,6 @@ static void jacobian(const orc_mech* m, ws_t* w, const orc_options* o, double p,
             for (int s = 0; s < nr; s++) Jc[R[s] * n + col] += v;
         }
         if (tb >= 0) {
-            const double dKrdC = dKfdC * invKc;
             const double* e = &m->eff[(size_t)tb * ns];
             for (int j = 0; j < ns; j++) {
                 const double Wd = (dKfdC * e[j]) * CF - (dKrdC * e[j]) * CR;
@@ -1533,8 +1565,8 @@ int32_t orc_tc(const orc_mech* m, int64_t n_cells, const double* p, const double
         arrhenius_rates(m, w, logT, invT, 0);
         third_body(m, w);
         for (int i = 0; i < m->nr; i++) {
-            if (m->kind[i] == FCS_RXN_THIRD_BODY) w->Kf[i] *= w->M[m->tbRow[i]];
-            else if (m->kind[i] >= FCS_RXN_LINDEMANN_FALLOFF) w->Kf[i] = falloff_rate(m, w, i, Tc, invT, NULL, NULL);
+            if (m->kind[i] == FCS_RXN_THIRD_BODY || m->kind[i] == FCS_RXN_NONEQ_THIRD_BODY) w->Kf[i] *= w->M[m->tbRow[i]];
+            else if (IS_FALLOFF(m->kind[i])) w->Kf[i] = falloff_rate(m, w, i, Tc, invT, NULL, NULL);
         }
         if (m->nPlog) plog_rates(m, w, p[c], logT, invT, 0);
         double sumW = 0, sumWR = 0;
@@ -1544,7 +1576,9 @@ int32_t orc_tc(const orc_mech* m, int64_t n_cells, const double* p, const double
             const int* R = &m->rSp[m->rOff[i]];
             const int nl = m->lOff[i + 1] - m->lOff[i], nr = m->rOff[i + 1] - m->rOff[i];
             double Kr = 0, Kp = 1.0;
-            if (m->rev[i]) {
+            /* Tc.C:578-600: the reverse rate only through Kc; a non-equilibrium
+             * reaction counts with its forward rate alone */
+            if (m->rev[i] == 1) {
                 for (int q = 0; q < nl; q++) Kp = Kp / w->B[L[q]];
                 for (int q = 0; q < nr; q++) Kp = Kp * w->B[R[q]];
                 double Kc = Kp * fast_pow(PByRT, nr - nl);

@@ -57,6 +57,8 @@ void fill_reaction(OptReaction& R, const fcs_mechanism_desc* d)
         else if (d->type[r] == FCS_RXN_THIRD_BODY) R.n_ThirdBodyReaction++;
         else if (d->type[r] == FCS_RXN_PLOG) R.n_PlogReaction++;
         else if (d->type[r] >= FCS_RXN_LINDEMANN_FALLOFF && d->type[r] <= FCS_RXN_SRI_FALLOFF) R.n_Fall_Off_Reaction++;
+        else if (d->type[r] == FCS_RXN_NONEQ) R.n_NonEquilibriumReversibleArrhenius++;
+        else if (d->type[r] == FCS_RXN_NONEQ_THIRD_BODY) R.n_NonEquilibriumThirdBodyReaction++;
         else throw std::runtime_error("unsupported reaction type in reference driver");
     }
     R.Itbr[0] = 0;
@@ -131,7 +133,35 @@ void fill_reaction(OptReaction& R, const fcs_mechanism_desc* d)
             iA++;
         }
     }
+    // non-equilibrium, then non-equilibrium third-body (OptReaction.C:610-700):
+    // forward rate at the reaction's slot, reverse at Ikf[9] onwards,
+    // isIrreversible = 2; the third-body kind takes forward row k and reverse
+    // row Itbr[4] + k, both from the forward coefficients as the reference reads them
+    unsigned jr = R.Ikf[9];
     unsigned k = 0;
+    for (int kind : {FCS_RXN_NONEQ, FCS_RXN_NONEQ_THIRD_BODY}) {
+        for (unsigned r = 0; r < nr; r++) {
+            if (d->type[r] != kind) continue;
+            R.isIrreversible[iA] = 2;
+            R.A[iA] = d->arrhenius[3 * r];
+            R.beta[iA] = d->arrhenius[3 * r + 1];
+            R.Ta[iA] = d->arrhenius[3 * r + 2];
+            R.A[jr] = d->arrhenius2[3 * r];
+            R.beta[jr] = d->arrhenius2[3 * r + 1];
+            R.Ta[jr] = d->arrhenius2[3 * r + 2];
+            if (kind == FCS_RXN_NONEQ_THIRD_BODY) {
+                R.ThirdBodyFactor[k].resize(ns);
+                R.ThirdBodyFactor[R.Itbr[4] + k].resize(ns);
+                for (unsigned s = 0; s < ns; s++) {
+                    R.ThirdBodyFactor[k][s] = d->efficiencies[(size_t)r * ns + s];
+                    R.ThirdBodyFactor[R.Itbr[4] + k][s] = d->efficiencies[(size_t)r * ns + s];
+                }
+                k++;
+            }
+            species(r, iA);
+            iA++; jr++;
+        }
+    }
     for (unsigned r = 0; r < nr; r++) {
         if (d->type[r] != FCS_RXN_THIRD_BODY) continue;
         if (!d->reversible[r]) R.isIrreversible[iA] = 1;
@@ -467,7 +497,7 @@ void* ref_create(const fcs_mechanism_desc* d, int solver, int jacobian, double a
     c.arrhenius2 = h->arr2.data(); c.falloff_params = h->fo.data();
     c.plog_offset = h->po.data(); c.plog_table = h->pt.data();
     for (int r = 0; r < nr; r++)
-        if (d->type[r] < FCS_RXN_ARRHENIUS || d->type[r] > FCS_RXN_SRI_FALLOFF) {
+        if (d->type[r] < FCS_RXN_ARRHENIUS || d->type[r] > FCS_RXN_NONEQ_THIRD_BODY) {
             delete h;
             return nullptr;
         }

@@ -35,6 +35,8 @@ CASES = [
     ("counterflow_53s", 4, "OptRosenbrock23"),
     ("falloff_16s", 64, "OptRodas34"),
     ("falloff_16s", 32, "OptSeulex"),
+    ("noneq_14s", 64, "OptRodas34"),
+    ("noneq_14s", 32, "OptSeulex"),
 ]
 
 
@@ -69,6 +71,7 @@ TC = [
     ("counterflow_53s", 64),
     ("uneven_111s", 64),
     ("falloff_16s", 64),
+    ("noneq_14s", 64),
 ]
 
 

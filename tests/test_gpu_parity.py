@@ -63,7 +63,7 @@ def test_exp_against_cuda(built):
 
 
 @pytest.mark.parametrize("wname,n", [("ignition_10s", 64), ("counterflow_53s", 32), ("uneven_111s", 16),
-                                     ("large_200s", 4), ("falloff_16s", 64)])
+                                     ("large_200s", 4), ("falloff_16s", 64), ("noneq_14s", 64)])
 def test_rhs_and_jacobian_match_oracle(built, wname, n):
     import oracle
     w, mech, flat, c = _setup(wname, n)
@@ -95,7 +95,8 @@ GOLDEN_CASES = ["ignition_10s_OptRodas34", "ignition_10s_OptRosenbrock34", "igni
                 "counterflow_53s_OptRodas34", "counterflow_53s_OptRosenbrock34", "counterflow_53s_OptSeulex",
                 "ignition_10s_OptRodas23", "ignition_10s_OptRosenbrock23",
                 "counterflow_53s_OptRodas23", "counterflow_53s_OptRosenbrock23",
-                "falloff_16s_OptRodas34", "falloff_16s_OptSeulex"]
+                "falloff_16s_OptRodas34", "falloff_16s_OptSeulex",
+                "noneq_14s_OptRodas34", "noneq_14s_OptSeulex"]
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
@@ -248,18 +249,23 @@ def test_rates_and_qdot_match_oracle(built):
     np.testing.assert_allclose(Q1, Q0, rtol=1e-10, atol=1e-12 * np.abs(Q0).max())
 
 
-def test_mechanism_from_openfoam_files(built, tmp_path):
+@pytest.mark.parametrize("wname", ["counterflow_53s", "falloff_16s", "noneq_14s"])
+def test_mechanism_from_openfoam_files(built, tmp_path, wname):
     """Loading the OpenFOAM reactions / speciesThermo dictionaries gives the
-    same chemistry as the flat description (incl. PLOG ArrheniusData and
-    third-body coefficient lists)."""
+    same chemistry as the flat description: PLOG ArrheniusData, third-body
+    coefficient lists, fall-off k0 / kInf / F / thirdBodyEfficiencies and
+    non-equilibrium forward / reverse entries."""
     from fcs import foam_io
-    w, mech, flat, c = _setup("counterflow_53s", 8)
+    w, mech, flat, c = _setup(wname, 8)
     paths = foam_io.write_case(mech, str(tmp_path))
     a = _ctx(flat)
     b = _ctx(flat)
     ns, nr = b.load_mechanism_foam(paths["reactions"], paths["thermo"])
-    assert (ns, nr) == (53, 325)
+    assert (ns, nr) == (mech.n_species, mech.n_reactions)
     np.testing.assert_allclose(b.rhs(c.p, c.T, c.Y), a.rhs(c.p, c.T, c.Y), rtol=1e-13, atol=0)
+    Ja, _ = a.jacobian(c.p, c.T, c.Y)
+    Jb, _ = b.jacobian(c.p, c.T, c.Y)
+    np.testing.assert_allclose(Jb, Ja, rtol=1e-13, atol=0)
 
 
 def test_queue_order_and_graph_replay_do_not_change_results(built):
@@ -300,7 +306,7 @@ def test_queue_order_and_graph_replay_do_not_change_results(built):
             assert s[k] == s0[k], k
 
 
-@pytest.mark.parametrize("wname", ["ignition_10s", "counterflow_53s", "uneven_111s", "falloff_16s"])
+@pytest.mark.parametrize("wname", ["ignition_10s", "counterflow_53s", "uneven_111s", "falloff_16s", "noneq_14s"])
 def test_tc_matches_reference_golden(built, wname):
     """fcs_tc against FastChemistryModel::tc() of the reference
     (tests/golden/tc.npz); differences are summation order and exp rounding."""
