@@ -11,6 +11,7 @@
 #include <cctype>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <map>
@@ -79,8 +80,15 @@ struct Lexer {
             if (quoted) *quoted = true;
             return out;
         }
+        // A word keeps balanced parentheses, as OpenFOAM's word tokens do
+        // (species such as CH2(S)); a ')' with no '(' open in the word ends it.
+        const bool word = std::isalpha((unsigned char)c) || c == '_';
+        int depth = 0;
         size_t j = i;
-        while (j < s.size() && !std::isspace((unsigned char)s[j]) && std::strchr("(){};[]\"", s[j]) == nullptr) {
+        while (j < s.size() && !std::isspace((unsigned char)s[j])) {
+            if (word && s[j] == '(') { depth++; j++; continue; }
+            if (word && s[j] == ')' && depth > 0) { depth--; j++; continue; }
+            if (std::strchr("(){};[]\"", s[j]) != nullptr) break;
             if (s[j] == '/' && j + 1 < s.size() && (s[j + 1] == '/' || s[j + 1] == '*')) break;
             j++;
         }
@@ -173,6 +181,24 @@ struct Parser {
                 if (!q3 && t == ";") break;
                 if (!q3 && t == "(") { val->items.push_back(parse_list(L)); continue; }
                 if (!q3 && t == "}") { err = "unexpected } in value of " + key; return; }
+                if (!q3 && t == "{") {
+                    // uniform list N{v}: N copies of one element (thermo databases
+                    // write unused coefficient sets as `7 { 0 }`)
+                    char* end = nullptr;
+                    const long count = val->items.empty() ? -1 : std::strtol(val->items.back()->tok.c_str(), &end, 10);
+                    if (count < 0 || count > 1000000 || !end || *end) { err = "bad uniform list in " + key; return; }
+                    bool q4 = false;
+                    std::string e = L.next(&q4);
+                    NodeP elem;
+                    if (!q4 && e == "(") elem = parse_list(L);
+                    else { elem = std::make_shared<Node>(); elem->tok = e; elem->quoted = q4; }
+                    if (L.next() != "}") { err = "bad uniform list in " + key; return; }
+                    auto lst = std::make_shared<Node>();
+                    lst->kind = Node::LIST;
+                    lst->items.assign((size_t)count, elem);
+                    val->items.back() = lst;
+                    continue;
+                }
                 auto tk = std::make_shared<Node>();
                 tk->tok = t;
                 tk->quoted = q3;
@@ -232,10 +258,13 @@ bool list_doubles(const Node* l, std::vector<double>& out) {
 
 }  // namespace
 
-struct fcs_ctx;
+namespace {
 
-extern "C" fcs_status fcs_load_mechanism_foam(fcs_ctx* ctx, const char* reactions_path, const char* thermo_path) {
-    if (!ctx || !reactions_path || !thermo_path) return FCS_ERR_INVALID;
+// Parses the reactions and thermo files into a flat description and hands it
+// (with the species names) to visit; the arrays live until visit returns.
+fcs_status parse_foam(const char* reactions_path, const char* thermo_path, fcs_mechanism_visitor visit,
+                      void* user) {
+    if (!reactions_path || !thermo_path || !visit) return FCS_ERR_INVALID;
     Parser P;
     Node rfile, tfile;
     if (!P.parse_file(reactions_path, rfile)) return FCS_ERR_PARSE;
@@ -400,7 +429,25 @@ extern "C" fcs_status fcs_load_mechanism_foam(fcs_ctx* ctx, const char* reaction
     d.lhs_offset = lo.data(); d.lhs_species = ls.data(); d.rhs_offset = ro.data(); d.rhs_species = rs.data();
     d.arrhenius = arr.data(); d.arrhenius2 = arr2.data(); d.efficiencies = eff.data();
     d.falloff_params = fp.data(); d.plog_offset = po.data(); d.plog_table = pt.data();
-    return fcs_load_mechanism(ctx, &d);
+    std::vector<const char*> names(ns);
+    for (int i = 0; i < ns; i++) names[i] = species[i].c_str();
+    return visit(&d, names.data(), user);
+}
+
+fcs_status load_visitor(const fcs_mechanism_desc* d, const char* const*, void* ctx) {
+    return fcs_load_mechanism(static_cast<fcs_ctx*>(ctx), d);
+}
+
+}  // namespace
+
+extern "C" fcs_status fcs_load_mechanism_foam(fcs_ctx* ctx, const char* reactions_path, const char* thermo_path) {
+    if (!ctx) return FCS_ERR_INVALID;
+    return parse_foam(reactions_path, thermo_path, load_visitor, ctx);
+}
+
+extern "C" fcs_status fcs_parse_mechanism_foam(const char* reactions_path, const char* thermo_path,
+                                               fcs_mechanism_visitor visit, void* user) {
+    return parse_foam(reactions_path, thermo_path, visit, user);
 }
 
 extern "C" fcs_status fcs_read_chemistry_properties(const char* path, fcs_options* o, double* initial_sub_dt) {

@@ -28,7 +28,8 @@ ERRORS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "STATE", 5: "CELLS", 
           7: "PARSE"}
 
 EXPORTS = ("fcs_create", "fcs_destroy", "fcs_last_error_string", "fcs_version", "fcs_load_mechanism",
-           "fcs_load_mechanism_foam", "fcs_read_chemistry_properties", "fcs_default_options",
+           "fcs_load_mechanism_foam", "fcs_parse_mechanism_foam", "fcs_read_chemistry_properties",
+           "fcs_default_options",
            "fcs_set_options", "fcs_mechanism_size", "fcs_integrate", "fcs_integrate_lts",
            "fcs_integrate_noalloc", "fcs_integrate_async", "fcs_sync", "fcs_rhs", "fcs_tc",
            "fcs_jacobian", "fcs_rates", "fcs_bench_fp64_peak", "fcs_bench_fp32_peak", "fcs_check_exp",
@@ -49,6 +50,9 @@ class MechDesc(C.Structure):
                 ("rhs_offset", _ip), ("rhs_species", _ip),
                 ("arrhenius", _dp), ("arrhenius2", _dp), ("efficiencies", _dp),
                 ("falloff_params", _dp), ("plog_offset", _ip), ("plog_table", _dp)]
+
+
+MechVisitor = C.CFUNCTYPE(C.c_int32, C.POINTER(MechDesc), C.POINTER(C.c_char_p), C.c_void_p)
 
 
 class Options(C.Structure):
@@ -113,6 +117,7 @@ def load(path: str = LIB) -> C.CDLL:
     L.fcs_version.restype = C.c_char_p
     L.fcs_load_mechanism.argtypes = [vp, C.POINTER(MechDesc)]
     L.fcs_load_mechanism_foam.argtypes = [vp, C.c_char_p, C.c_char_p]
+    L.fcs_parse_mechanism_foam.argtypes = [C.c_char_p, C.c_char_p, MechVisitor, vp]
     L.fcs_read_chemistry_properties.argtypes = [C.c_char_p, C.POINTER(Options), _dp]
     L.fcs_default_options.argtypes = [C.POINTER(Options)]
     L.fcs_set_options.argtypes = [vp, C.POINTER(Options)]
@@ -160,13 +165,24 @@ class FcsError(RuntimeError):
         self.code = code
 
 
+def _host64(a) -> np.ndarray:
+    """A C-contiguous float64 host array (the argument itself when it already is one)."""
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
 def _addr(a):
-    """Address of a numpy array or a torch tensor (None -> NULL)."""
+    """Address of a C-contiguous numpy array or torch tensor (None -> NULL).
+    The caller keeps the array alive for the whole C call; a strided view is
+    refused rather than read with the wrong layout."""
     if a is None:
         return None
     if isinstance(a, np.ndarray):
+        if not a.flags.c_contiguous:
+            raise ValueError("array arguments must be C-contiguous")
         return a.ctypes.data
-    return a.data_ptr()  # torch tensor
+    if not a.is_contiguous():  # torch tensor
+        raise ValueError("tensor arguments must be contiguous")
+    return a.data_ptr()
 
 
 def make_desc(flat) -> MechDesc:
@@ -222,6 +238,41 @@ def check_exp(x, device: int = 0):
     if st:
         raise FcsError(st, "exp check failed")
     return a, b
+
+
+def parse_mechanism_foam(reactions_path: str, thermo_path: str):
+    """The mechanism of an OpenFOAM ``reactions`` + thermo file pair as the
+    library reads it (fcs_parse_mechanism_foam; host only, no GPU):
+    returns (FlatMechanism, species names)."""
+    from .mechanism import FlatMechanism
+    L = load()
+    got = {}
+
+    def visit(dp, names, _user):
+        d = dp.contents
+        ns, nr = d.n_species, d.n_reactions
+
+        def arr(ptr, n, dtype):
+            return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True) if n else np.zeros(0, dtype)
+        lo = arr(d.lhs_offset, nr + 1, np.int32)
+        ro = arr(d.rhs_offset, nr + 1, np.int32)
+        po = arr(d.plog_offset, nr + 1, np.int32)
+        got["flat"] = FlatMechanism(
+            ns, nr, arr(d.W, ns, np.float64), arr(d.T_low, ns, np.float64), arr(d.T_high, ns, np.float64),
+            arr(d.T_common, ns, np.float64), arr(d.high_coeffs, 7 * ns, np.float64),
+            arr(d.low_coeffs, 7 * ns, np.float64), arr(d.type, nr, np.int32), arr(d.reversible, nr, np.int32),
+            lo, arr(d.lhs_species, int(lo[-1]), np.int32), ro, arr(d.rhs_species, int(ro[-1]), np.int32),
+            arr(d.arrhenius, 3 * nr, np.float64), arr(d.arrhenius2, 3 * nr, np.float64),
+            arr(d.efficiencies, nr * ns, np.float64), arr(d.falloff_params, 5 * nr, np.float64),
+            po, arr(d.plog_table, 4 * max(int(po[-1]), 1), np.float64))
+        got["names"] = [names[i].decode() for i in range(ns)]
+        return 0
+
+    cb = MechVisitor(visit)
+    st = L.fcs_parse_mechanism_foam(reactions_path.encode(), thermo_path.encode(), cb, None)
+    if st:
+        raise FcsError(st, f"cannot read {reactions_path} / {thermo_path}")
+    return got["flat"], got["names"]
 
 
 def read_chemistry_properties(path: str):
@@ -344,37 +395,37 @@ class Context:
                                              dt_per_cell=dtc)
         return dict(T=T, Y=Y, subDt=sub, RR=RR, status=status, deltaTMin=dmin, stats=stats, code=st)
 
+    # The contiguous float64 copies are bound to locals for the whole call:
+    # an address taken from a temporary copy would dangle once the copy is freed.
     def rhs(self, p, T, Y):
+        p, T, Y = _host64(p), _host64(T), _host64(Y)
         n = T.shape[0]
         out = np.zeros((self.ns + 1, n))
-        self._check(self.L.fcs_rhs(self.h, n, _addr(np.ascontiguousarray(p)), _addr(np.ascontiguousarray(T)),
-                                   _addr(np.ascontiguousarray(Y)), _addr(out), 0))
+        self._check(self.L.fcs_rhs(self.h, n, _addr(p), _addr(T), _addr(Y), _addr(out), 0))
         return out
 
     def jacobian(self, p, T, Y):
+        p, T, Y = _host64(p), _host64(T), _host64(Y)
         n = T.shape[0]
         N = self.ns + 1
         J = np.zeros((n, N, N))
         f = np.zeros((N, n))
-        self._check(self.L.fcs_jacobian(self.h, n, _addr(np.ascontiguousarray(p)),
-                                        _addr(np.ascontiguousarray(T)), _addr(np.ascontiguousarray(Y)),
-                                        _addr(J), _addr(f), 0))
+        self._check(self.L.fcs_jacobian(self.h, n, _addr(p), _addr(T), _addr(Y), _addr(J), _addr(f), 0))
         return J, f
 
     def tc(self, p, T, rho, Y):
+        p, T, rho, Y = _host64(p), _host64(T), _host64(rho), _host64(Y)
         n = T.shape[0]
         out = np.zeros(n)
-        self._check(self.L.fcs_tc(self.h, n, _addr(np.ascontiguousarray(p)), _addr(np.ascontiguousarray(T)),
-                                  _addr(np.ascontiguousarray(rho)), _addr(np.ascontiguousarray(Y)), _addr(out), 0))
+        self._check(self.L.fcs_tc(self.h, n, _addr(p), _addr(T), _addr(rho), _addr(Y), _addr(out), 0))
         return out
 
     def rates(self, p, T, rho, Y):
+        p, T, rho, Y = _host64(p), _host64(T), _host64(rho), _host64(Y)
         n = T.shape[0]
         RR = np.zeros((self.ns, n))
         Q = np.zeros(n)
-        self._check(self.L.fcs_rates(self.h, n, _addr(np.ascontiguousarray(p)), _addr(np.ascontiguousarray(T)),
-                                     _addr(np.ascontiguousarray(rho)), _addr(np.ascontiguousarray(Y)),
-                                     _addr(RR), _addr(Q), 0))
+        self._check(self.L.fcs_rates(self.h, n, _addr(p), _addr(T), _addr(rho), _addr(Y), _addr(RR), _addr(Q), 0))
         return RR, Q
 
 

@@ -198,6 +198,16 @@ fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc* desc);
 fcs_status fcs_load_mechanism_foam(fcs_ctx* ctx, const char* reactions_path,
                                    const char* thermo_path);
 
+/* Host only (no context, no device): parses the same two files as
+ * fcs_load_mechanism_foam and hands the flat description and the species
+ * names (thermo-file order) to `visit`, whose status is returned.  The arrays
+ * are valid during the call only.  For callers that inspect, convert or keep
+ * a mechanism without loading it. */
+typedef fcs_status (*fcs_mechanism_visitor)(const fcs_mechanism_desc* desc,
+                                            const char* const* species_names, void* user);
+fcs_status fcs_parse_mechanism_foam(const char* reactions_path, const char* thermo_path,
+                                    fcs_mechanism_visitor visit, void* user);
+
 /* Reads the chemistryProperties keys of the plugin (FastChemistryModel.C:45-168,
  * OptRodas34.C:34-50) into opts: chemistryType{solver}, jacobian, Treact,
  * <Solver>Coeffs{absTol,relTol,maxSteps}, maxChemicalTimeStep and the optional

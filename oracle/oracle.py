@@ -19,6 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libfcs_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libfcs_ref.so")
 REF_SRC = "/root/reference/src"
+REF_TUTORIAL = os.path.join(os.path.dirname(REF_SRC), "tutorial")  # mechanisms + cases
 
 SOLVERS = {"OptRodas34": 0, "OptRosenbrock34": 1, "OptSeulex": 2, "OptRodas23": 3, "OptRosenbrock23": 4}
 

@@ -50,3 +50,16 @@ def test_no_cpu_fallback_when_library_missing(tmp_path):
             _lib.load(str(tmp_path / "missing.so"))
     finally:
         _lib._LIB = saved
+
+
+def test_binding_refuses_strided_arrays():
+    """A strided view handed to the C ABI would be read with the wrong layout:
+    the binding refuses it (the evaluation helpers copy their inputs first)."""
+    import numpy as np
+    import pytest
+    from fcs import _lib
+    a = np.zeros((4, 6))
+    assert _lib._addr(a) == a.ctypes.data
+    with pytest.raises(ValueError):
+        _lib._addr(a[:, ::2])
+    assert _lib._host64(a[:, ::2]).flags.c_contiguous

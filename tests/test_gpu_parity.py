@@ -249,6 +249,21 @@ def test_rates_and_qdot_match_oracle(built):
     np.testing.assert_allclose(Q1, Q0, rtol=1e-10, atol=1e-12 * np.abs(Q0).max())
 
 
+def test_strided_host_inputs(built):
+    """Views with strides (a column slice of a species-major field) give the
+    same rates, Jacobian and tc as contiguous copies."""
+    w, mech, flat, c = _setup("noneq_14s", 32)
+    ctx = _ctx(flat)
+    p, T, rho, Y = c.p[::2], c.T[::2], c.rho0[::2], c.Y[:, ::2]
+    pc, Tc, rc, Yc = (np.ascontiguousarray(a) for a in (p, T, rho, Y))
+    np.testing.assert_array_equal(ctx.rhs(p, T, Y), ctx.rhs(pc, Tc, Yc))
+    J0, f0 = ctx.jacobian(pc, Tc, Yc)
+    J1, f1 = ctx.jacobian(p, T, Y)
+    np.testing.assert_array_equal(J1, J0)
+    np.testing.assert_array_equal(ctx.tc(p, T, rho, Y), ctx.tc(pc, Tc, rc, Yc))
+    np.testing.assert_array_equal(ctx.rates(p, T, rho, Y)[0], ctx.rates(pc, Tc, rc, Yc)[0])
+
+
 @pytest.mark.parametrize("wname", ["counterflow_53s", "falloff_16s", "noneq_14s"])
 def test_mechanism_from_openfoam_files(built, tmp_path, wname):
     """Loading the OpenFOAM reactions / speciesThermo dictionaries gives the
