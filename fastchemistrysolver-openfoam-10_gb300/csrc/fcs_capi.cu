@@ -196,21 +196,21 @@ extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc*
         const int r0 = d->rhs_offset[r], r1 = d->rhs_offset[r + 1];
         if (l1 - l0 < 1 || r1 - r0 < 1)
             return set_err(ctx, FCS_ERR_INVALID, "reaction without reactants or products");
-        if (l1 - l0 > kMaxSide || r1 - r0 > kMaxSide)
-            return set_err(ctx, FCS_ERR_UNSUPPORTED, "reactions with more than 3 reactants or products "
-                                                     "(the reference's RFG/JFG path) are not supported");
+        if (l1 - l0 > kMaxL || r1 - r0 > kMaxR)
+            return set_err(ctx, FCS_ERR_UNSUPPORTED, "reactions with more than 4 reactants or 8 products "
+                                                     "are not supported by the GPU path");
         x.nl = int8_t(l1 - l0);
         x.nr = int8_t(r1 - r0);
         for (int q = 0; q < x.nl; q++) {
             const int sp = d->lhs_species[l0 + q];
             if (sp < 0 || sp >= ns) return set_err(ctx, FCS_ERR_INVALID, "species index out of range");
-            x.sl[q] = int16_t(sp);
+            x.sl[q] = uint8_t(sp);
             inc[sp].push_back(k << 1);
         }
         for (int q = 0; q < x.nr; q++) {
             const int sp = d->rhs_species[r0 + q];
             if (sp < 0 || sp >= ns) return set_err(ctx, FCS_ERR_INVALID, "species index out of range");
-            x.sr[q] = int16_t(sp);
+            x.sr[q] = uint8_t(sp);
             inc[sp].push_back((k << 1) | 1);
         }
         const bool noneq = d->type[r] == FCS_RXN_NONEQ || d->type[r] == FCS_RXN_NONEQ_THIRD_BODY;

@@ -352,29 +352,63 @@ __device__ __forceinline__ double fast_exp(double x) {
     return __longlong_as_double(__double_as_longlong(res) + ((N >> 6) << 52));
 }
 
-// (Pstd/(Ru T))^(-dnu) for dnu = -2..2: the pressure factor of 1/Kc
-struct PFactor { double v[5]; };
+// OptReaction::fastPow (OptReaction.H:1405-1420)
+__device__ __forceinline__ double fast_pow_int(double x, int order) {
+    double xx = order < 0 ? 1 / x : x;
+    double y = 1;
+    for (int i = order; i != 0; i /= 2) {
+        if (i % 2) y *= xx;
+        xx *= xx;
+    }
+    return y;
+}
+
+// Pstd/(Ru T) and its inverse: the pressure factor of 1/Kc is (Pstd/(Ru T))^(-dnu)
+struct PFactor { double P, invP; };
 
 __device__ __forceinline__ PFactor pressure_factors(double Tc) {
-    const double invPByRT = kRu * Tc / kPstd;
-    const double PByRT = 1.0 / invPByRT;
     PFactor f;
-    f.v[0] = PByRT * PByRT; f.v[1] = PByRT; f.v[2] = 1.0; f.v[3] = invPByRT; f.v[4] = invPByRT * invPByRT;
+    f.invP = kRu * Tc / kPstd;
+    f.P = 1.0 / f.invP;
     return f;
 }
 
 constexpr double kInvKcClamp = 1.0 / kKcClamp;
+constexpr double kInvKcClampG = 1.0 / kKcClampG;
+
+// (Pstd/(Ru T))^(-dnu): the reference's table for |dnu| <= 2
+// (ChemicalEquilibriumFunctionI.H:14-25), fastPow beyond it (RFG/JFG)
+__device__ __forceinline__ double pressure_factor(const PFactor& pf, int dnu) {
+    switch (dnu) {
+        case -2: return pf.P * pf.P;
+        case -1: return pf.P;
+        case 1: return pf.invP;
+        case 2: return pf.invP * pf.invP;
+        default: return fast_pow_int(pf.invP, dnu);
+    }
+}
+
+// The clamp of 1/Kc: RFG/JFG (more than 3 species on a side) use the other constant
+__device__ __forceinline__ double inv_kc_clamp(const RxnInfo& x) {
+    return (x.nl > 3 || x.nr > 3) ? kInvKcClampG : kInvKcClamp;
+}
 
 // 1/Kc from per-species exp(-G/RT) and its inverse, no division:
 // 1/Kc = prod_reactants E * prod_products 1/E * (Pstd/(Ru T))^-dnu, with the
-// reference's lower clamp of Kc (ReactionFunctionI.H:17) as an upper clamp.
+// reference's lower clamp of Kc (ReactionFunctionI.H:17; RFG's for more than
+// 3 species on a side) as an upper clamp.
 __device__ __forceinline__ double inv_equilibrium_kc(const RxnInfo& x, const double* E, const double* Einv,
                                                      const PFactor& pf) {
     double v = E[x.sl[0]];
+    // Species loops over a reaction stay rolled: unrolled over the 4 + 8 byte
+    // slots of RxnInfo they raised the integrator's register spills.
+    #pragma unroll 1
     for (int q = 1; q < x.nl; q++) v *= E[x.sl[q]];
+    #pragma unroll 1
     for (int q = 0; q < x.nr; q++) v *= Einv[x.sr[q]];
-    if (x.dnu != 0) v *= pf.v[x.dnu + 2];
-    return v > kInvKcClamp ? kInvKcClamp : v;
+    if (x.dnu != 0) v *= pressure_factor(pf, x.dnu);
+    const double cl = inv_kc_clamp(x);
+    return v > cl ? cl : v;
 }
 
 // ------------------------------------------------------------------------
@@ -621,8 +655,10 @@ __device__ __noinline__ void rhs_eval(const Grp<G>& g, const DevMech& M, const S
     // Arrhenius.
     auto finish = [&](const int r, const RxnInfo& x, const double Kf, const double Kr) {
         double CF = s.C[x.sl[0]];
+        #pragma unroll 1
         for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
         double CR = s.C[x.sr[0]];
+        #pragma unroll 1
         for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
         s.q[r] = Kf * CF - Kr * CR;
     };
@@ -679,17 +715,6 @@ __device__ __noinline__ void rhs_eval(const Grp<G>& g, const DevMech& M, const S
 // 1.49011611938476e-8; tc = sum(w) / sum(w^2) * sum(c).  Returns tc to every
 // thread.
 
-// OptReaction::fastPow (OptReaction.H:1405-1420)
-__device__ __forceinline__ double fast_pow_int(double x, int order) {
-    double xx = order < 0 ? 1 / x : x;
-    double y = 1;
-    for (int i = order; i != 0; i /= 2) {
-        if (i % 2) y *= xx;
-        xx *= xx;
-    }
-    return y;
-}
-
 template<int G, class MT>
 __device__ __noinline__ double tc_eval(const Grp<G>& g, const DevMech& M, const Slot<MT>& s, double p, double T,
                                        double rho, const double* Y) {
@@ -726,15 +751,19 @@ __device__ __noinline__ double tc_eval(const Grp<G>& g, const DevMech& M, const 
         double Kr = 0;
         if (x.rev == 1) {
             double Kp = 1.0;
+            #pragma unroll 1
             for (int q = 0; q < x.nl; q++) Kp = Kp / s.B[x.sl[q]];
+            #pragma unroll 1
             for (int q = 0; q < x.nr; q++) Kp = Kp * s.B[x.sr[q]];
             double Kc = Kp * fast_pow_int(PByRT, x.dnu);
             Kc = Kc > 1.49011611938476e-8 ? Kc : 1.49011611938476e-8;
             Kr = Kf / Kc;
         }
         double CF = s.C[x.sl[0]];
+        #pragma unroll 1
         for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
         double CR = s.C[x.sr[0]];
+        #pragma unroll 1
         for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
         const double wf = x.nr * (Kf * CF), wr = x.nl * (Kr * CR);
         sw += wf + wr;
@@ -797,8 +826,10 @@ __device__ __noinline__ double rates_eval(const Grp<G>& g, const DevMech& M, con
     // Arrhenius.
     auto finish = [&](const int r, const RxnInfo& x, const double Kf, const double Kr) {
         double CF = s.C[x.sl[0]];
+        #pragma unroll 1
         for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
         double CR = s.C[x.sr[0]];
+        #pragma unroll 1
         for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
         s.q[r] = Kf * CF - Kr * CR;
     };
@@ -918,20 +949,24 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
                           double& Kr, double& dKrdT, double& dKrdC) {
         const double invKc = inv_equilibrium_kc(x, s.B, s.Binv, pf);
         double sv = s.dBdT[x.sr[0]];
+        #pragma unroll 1
         for (int q = 1; q < x.nr; q++) sv += s.dBdT[x.sr[q]];
         double sl = s.dBdT[x.sl[0]];
+        #pragma unroll 1
         for (int q = 1; q < x.nl; q++) sl += s.dBdT[x.sl[q]];
         const double dKcdTByKc = (sv - sl) - x.dnu * invT;
         Kr = Kf * invKc;
         // the Kc term of dKr/dT is dropped when Kc sits on its clamp (JacobianFunctionI.H:246-249)
-        dKrdT = dKfdT * invKc - (invKc < kInvKcClamp ? Kr * dKcdTByKc : 0.0);
+        dKrdT = dKfdT * invKc - (invKc < inv_kc_clamp(x) ? Kr * dKcdTByKc : 0.0);
         dKrdC = dKfdC * invKc;
     };
     auto finish = [&](const int r, const RxnInfo& x, const double Kf, const double dKfdT, const double dKfdC,
                       const double Kr, const double dKrdT, const double dKrdC) {
         double CF = s.C[x.sl[0]];
+        #pragma unroll 1
         for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
         double CR = s.C[x.sr[0]];
+        #pragma unroll 1
         for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
         s.Kf[r] = Kf;
         s.Kr[r] = Kr;
@@ -987,6 +1022,7 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
                 // forward: Kf * product of the other reactant concentrations
                 bool skipped = false;
                 d = s.Kf[r];
+                #pragma unroll 1
                 for (int q = 0; q < x.nl; q++) {
                     if (!skipped && x.sl[q] == j) { skipped = true; continue; }
                     d *= s.C[x.sl[q]];
@@ -995,13 +1031,16 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
                 if (!x.rev) continue;
                 bool skipped = false;
                 d = -s.Kr[r];
+                #pragma unroll 1
                 for (int q = 0; q < x.nr; q++) {
                     if (!skipped && x.sr[q] == j) { skipped = true; continue; }
                     d *= s.C[x.sr[q]];
                 }
             }
             const MT md = MT(d);
+            #pragma unroll 1
             for (int q = 0; q < x.nl; q++) { MT& c = J[(size_t)x.sl[q] * ld + j]; c = c - md; }
+            #pragma unroll 1
             for (int q = 0; q < x.nr; q++) { MT& c = J[(size_t)x.sr[q] * ld + j]; c = c + md; }
         }
     }

@@ -20,14 +20,17 @@ namespace fcs {
 constexpr double kRu = 8314.470066505449722171761095523834228515625;  // OptReaction.H:404
 constexpr double kPstd = 100000.0;                                    // OptReaction.H:409
 constexpr double kKcClamp = 1.4901171103413047e-8;                    // ReactionFunctionI.H:17
+constexpr double kKcClampG = 1.49011611938476e-8;                     // RFG/JFG: more than 3 per side
 constexpr double kPivEps = 2.2204460492503131e-16;                    // LUsolver.C:154
 constexpr double kSmall = 1.0e-15;                                    // OpenFOAM small
-constexpr int kMaxSide = 3;  // reactants/products per reaction handled on the GPU
+// reactants / products per reaction handled on the GPU (species indices are
+// bytes: at most 255 species); the tutorial mechanisms have at most 3 / 7
+constexpr int kMaxL = 4, kMaxR = 8;
 
 struct RxnInfo {            // 64 bytes
     double A, beta, Ta;     // Arrhenius (OpenFOAM form k = A T^beta exp(-Ta/T))
-    int16_t sl[kMaxSide];   // reactant species (repeated by stoichiometry)
-    int16_t sr[kMaxSide];   // product species
+    uint8_t sl[kMaxL];      // reactant species (repeated by stoichiometry)
+    uint8_t sr[kMaxR];      // product species
     int8_t nl, nr;          // counts
     int8_t rev;             // 1 reversible (Kr = Kf / Kc), 2 non-equilibrium (Kr its own Arrhenius)
     int8_t kind;            // FCS_RXN_*

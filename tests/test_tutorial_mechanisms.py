@@ -5,7 +5,8 @@ CFD step of ignition-like cells with Rodas34.
 
 Together the mechanisms cover every reaction kind the tutorials use:
 (ir)reversible Arrhenius, third-body, Lindemann / Troe / SRI fall-off, PLOG
-and non-equilibrium (third-body) reactions, species names with parentheses
+and non-equilibrium (third-body) reactions, reactions with more than three
+products (the reference's generic RFG/JFG path), species names with parentheses
 (CH2(S)) and thermo databases with uniform lists.  The tests run where the
 reference tree and its compiled core are present (the x86-64 build host) and
 skip elsewhere; no mechanism data is stored in this repository.
@@ -25,6 +26,9 @@ MECHS = [
     ("Ignition0D/C2H4_Zettervall2024", "C2H4"),    # irreversible fall-off
     ("Ignition0D/DME_LLNL", "CH3OCH3"),            # non-equilibrium, 79 species
     ("Ignition0D/NH3CH4_Konnov", "NH3"),           # SRI, 129 species / 1231 reactions
+    ("Ignition0D/C3H8_Qin2000", "C3H8"),           # a reversible reaction with 4 products
+    ("Ignition0D/Kerosene_Zettervall2020", "C12H22"),  # global reactions with up to 7 products
+    ("Ignition0D/NC12H26_Gao2014", "NC12H26"),     # 15 reactions with 4 products
 ]
 
 
