@@ -333,7 +333,7 @@ bool fcs::make_shape(fcs_ctx* ctx, int group, bool integrate, Shape& sh) {
     const bool mixed = o.precision == FCS_PRECISION_MIXED;
     const bool seulex = integrate && o.solver == FCS_SOLVER_SEULEX;
     sh.mixed = mixed;
-    sh.L = make_layout(ctx->M.ns, ctx->M.nr, ctx->M.nTB, mixed, seulex);
+    sh.L = make_layout(ctx->M.ns, ctx->M.nr, ctx->M.nTB, mixed, seulex, group);
     sh.lc.group = group;
     if (ctx->M.n > 256) return false;  // the solves keep <= 256 unknowns per warp lane set
     const size_t smemCap = ctx->maxSmemPerBlock;

@@ -154,7 +154,9 @@ struct SlotLayout {
     int offInvD;       // [n] double
     int offScale;      // row / column equilibration factors [2n] double (mixed precision)
     int offPiv;        // [n] int
-    int offRx;         // Kf, Kr, q, dqdT [nr] each
+    int offRx;         // Kf, Kr, q, dqdT [rc] each: one chunk of reactions
+    int rc;            // reactions per chunk (2 G, at most nr)
+    int offCur;        // [ns] int: per-species incidence cursor across chunks
     int offTb;         // M, dKfdC, dKrdC, CF, CR [nTB] each
     int offTable;      // Seulex extrapolation table [12][n] doubles
     int offRed;        // 48 doubles of reduction / broadcast scratch
@@ -171,7 +173,7 @@ __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 //   mixed Rosenbrock: FP32 Jacobian + FP32 LU; the FP64 view (Jacobian assembly in
 //                     FP64, and the FP64 fallback attempt) overlays both
 //   mixed Seulex    : as FP64 Seulex, with the two FP32 matrices inside the FP64 Jacobian
-__host__ __device__ inline SlotLayout make_layout(int ns, int nr, int nTB, bool mixed, bool seulex) {
+__host__ __device__ inline SlotLayout make_layout(int ns, int nr, int nTB, bool mixed, bool seulex, int group) {
     SlotLayout L;
     const int n = ns + 1;
     L.ld = n | 1;
@@ -184,12 +186,14 @@ __host__ __device__ inline SlotLayout make_layout(int ns, int nr, int nTB, bool 
     L.offJ32 = 0;                                    // (unused: the Jacobian stays FP64)
     L.offLU32 = m64;                                 // after the FP64 Jacobian (inside LU64 for Seulex)
     L.offVec = o;   o = align16(o + kNV * n * 8);
-    L.offVec32 = o; o = align16(o + 2 * n * 4);
+    L.offVec32 = o; if (mixed) o = align16(o + 2 * n * 4);
     L.offSp = o;    o = align16(o + 7 * ns * 8);
     L.offInvD = o;  o = align16(o + n * 8);
-    L.offScale = o; o = align16(o + 2 * n * 8);
+    L.offScale = o; if (mixed) o = align16(o + 2 * n * 8);
     L.offPiv = o;   o = align16(o + n * 4);
-    L.offRx = o;    o = align16(o + 4 * nr * 8);
+    L.rc = nr < 2 * group ? (nr > 0 ? nr : 1) : 2 * group;
+    L.offRx = o;    o = align16(o + 4 * L.rc * 8);
+    L.offCur = o;   o = align16(o + ns * 4);
     L.offTb = o;    o = align16(o + 5 * (nTB > 0 ? nTB : 1) * 8);
     L.offTable = o;
     if (seulex) o = align16(o + 12 * n * 8);
@@ -210,7 +214,9 @@ struct Slot {
     double* invD;
     double *dr, *dc;
     int* piv;
-    double *Kf, *Kr, *q, *dqdT;
+    double *Kf, *Kr, *q, *dqdT;   // one chunk of reactions: index r - c0
+    int rc;                        // reactions per chunk
+    int* cur;                      // per-species incidence cursor
     double *Mtb, *tbF, *tbR, *tbCF, *tbCR;
     double* table;
     double* red;
@@ -240,7 +246,9 @@ __device__ __forceinline__ Slot<MT> make_slot(char* base, const SlotLayout& L, c
     s.dc = s.dr + M.n;
     s.piv = reinterpret_cast<int*>(base + L.offPiv);
     double* rx = reinterpret_cast<double*>(base + L.offRx);
-    s.Kf = rx; s.Kr = rx + M.nr; s.q = rx + 2 * M.nr; s.dqdT = rx + 3 * M.nr;
+    s.rc = L.rc;
+    s.Kf = rx; s.Kr = rx + L.rc; s.q = rx + 2 * L.rc; s.dqdT = rx + 3 * L.rc;
+    s.cur = reinterpret_cast<int*>(base + L.offCur);
     double* tb = reinterpret_cast<double*>(base + L.offTb);
     const int nt = M.nTB > 0 ? M.nTB : 1;
     s.Mtb = tb; s.tbF = tb + nt; s.tbR = tb + 2 * nt; s.tbCF = tb + 3 * nt; s.tbCR = tb + 4 * nt;
@@ -604,6 +612,96 @@ static __device__ __forceinline__ SpecialK special_rates(const DevMech& M, const
 }
 
 // ------------------------------------------------------------------------
+// Reactions are evaluated in chunks of s.rc (2 G) so that the per-reaction
+// arrays of a cell slot hold one chunk, not the whole mechanism: the slot
+// then fits more cells per SM.  Every sum keeps its order: a species' terms
+// are added in reaction order across the chunks, its incidence cursor
+// (s.cur) carrying over from one chunk to the next.
+
+// Net rates q of the reactions [c0, c1) into s.q[r - c0] (ReactionRate.C:521-575
+// and the RF* functions).  The special block [spBegin, spBegin + nSp) of the
+// packed order (first non-equilibrium to last fall-off reaction) runs in a
+// loop of its own, so that the main loop carries neither the fall-off call
+// nor a second Arrhenius.
+template<int G, class MT>
+__device__ __forceinline__ void net_rates_chunk(const Grp<G>& g, const DevMech& M, const Slot<MT>& s, double p,
+                                                double logP, double Tc, double logT, double invT,
+                                                const PFactor& pf, int c0, int c1) {
+    const int sp0 = M.spBegin, sp1 = M.spBegin + M.nSp;
+    auto finish = [&](const int r, const RxnInfo& x, const double Kf, const double Kr) {
+        double CF = s.C[x.sl[0]];
+        #pragma unroll 1
+        for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
+        double CR = s.C[x.sr[0]];
+        #pragma unroll 1
+        for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
+        s.q[r - c0] = Kf * CF - Kr * CR;
+    };
+    for (int r = c0 + g.rank; r < c1; r += G) {
+        if (r >= sp0 && r < sp1) continue;
+        const RxnInfo x = load_rx(M.rx + r);
+        double Kf;
+        if (x.kind == FCS_RXN_PLOG) {
+            double dk;
+            Kf = plog_rate(M, x.plog, p, logP, logT, invT, &dk);
+        } else if (x.tind) {
+            Kf = x.A;
+        } else {
+            Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
+        }
+        if (x.tb >= 0) Kf *= s.Mtb[x.tb];
+        double Kr = 0;
+        if (x.rev) Kr = Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
+        finish(r, x, Kf, Kr);
+    }
+    for (int r = max(c0, sp0) + g.rank; r < min(c1, sp1); r += G) {
+        const RxnInfo x = load_rx(M.rx + r);
+        const SpecialK k = special_rates(M, x, s.Mtb, Tc, logT, invT, false);
+        double Kr = k.Kr;  // non-equilibrium: its own reverse rate
+        if (x.rev == 1) Kr = k.Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
+        finish(r, x, k.Kf, Kr);
+    }
+}
+
+// acc[i] += the net rates of the chunk [c0, c1) for species i (+q as a
+// product, -q as a reactant), in reaction order.
+template<int G, class MT>
+__device__ __forceinline__ void gather_chunk(const Grp<G>& g, const DevMech& M, const Slot<MT>& s, int c0, int c1,
+                                             double* acc) {
+    for (int i = g.rank; i < M.ns; i += G) {
+        double w = acc[i];
+        int e = s.cur[i];
+        const int e1 = __ldg(&M.incOff[i + 1]);
+        for (; e < e1; e++) {
+            const int v = __ldg(&M.inc[e]);
+            if ((v >> 1) >= c1) break;
+            const double qq = s.q[(v >> 1) - c0];
+            w = (v & 1) ? w + qq : w - qq;
+        }
+        s.cur[i] = e;
+        acc[i] = w;
+    }
+}
+
+// Sum over the chunks: acc[i] = w_i for every species.
+template<int G, class MT>
+__device__ __forceinline__ void net_production(const Grp<G>& g, const DevMech& M, const Slot<MT>& s, double p,
+                                               double logP, double Tc, double logT, double invT,
+                                               const PFactor& pf, double* acc) {
+    for (int i = g.rank; i < M.ns; i += G) {
+        s.cur[i] = __ldg(&M.incOff[i]);
+        acc[i] = 0.0;
+    }
+    for (int c0 = 0; c0 < M.nr; c0 += s.rc) {
+        const int c1 = min(M.nr, c0 + s.rc);
+        net_rates_chunk<G, MT>(g, M, s, p, logP, Tc, logT, invT, pf, c0, c1);
+        g.sync();
+        gather_chunk<G, MT>(g, M, s, c0, c1, acc);
+        if (c1 < M.nr) g.sync();  // the next chunk overwrites q
+    }
+}
+
+// ------------------------------------------------------------------------
 // right-hand side: FastChemistryModel::derivatives (FastChemistryModel.C:194-273
 // for mode 1, 340-417 for mode 2) over OptReaction::dNdtByV
 // (ReactionRate.C:732-1503).  YT is clamped (Y >= 0) in place.
@@ -649,54 +747,10 @@ __device__ __noinline__ void rhs_eval(const Grp<G>& g, const DevMech& M, const S
     g.sync();
     const PFactor pf = pressure_factors(Tc);
     const double logP = M.nPlog ? log(p) : 0.0;
-    // The special block [spBegin, spBegin + nSp) of the packed order (first
-    // non-equilibrium to last fall-off reaction) runs in a loop of its own, so
-    // that the main loop carries neither the fall-off call nor a second
-    // Arrhenius.
-    auto finish = [&](const int r, const RxnInfo& x, const double Kf, const double Kr) {
-        double CF = s.C[x.sl[0]];
-        #pragma unroll 1
-        for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
-        double CR = s.C[x.sr[0]];
-        #pragma unroll 1
-        for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
-        s.q[r] = Kf * CF - Kr * CR;
-    };
-    for (int j = g.rank; j < M.nr - M.nSp; j += G) {
-        const int r = j < M.spBegin ? j : j + M.nSp;
-        const RxnInfo x = load_rx(M.rx + r);
-        double Kf;
-        if (x.kind == FCS_RXN_PLOG) {
-            double dk;
-            Kf = plog_rate(M, x.plog, p, logP, logT, invT, &dk);
-        } else if (x.tind) {
-            Kf = x.A;
-        } else {
-            Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
-        }
-        if (x.tb >= 0) Kf *= s.Mtb[x.tb];
-        double Kr = 0;
-        if (x.rev) Kr = Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
-        finish(r, x, Kf, Kr);
-    }
-    for (int r = M.spBegin + g.rank; r < M.spBegin + M.nSp; r += G) {
-        const RxnInfo x = load_rx(M.rx + r);
-        const SpecialK k = special_rates(M, x, s.Mtb, Tc, logT, invT, false);
-        double Kr = k.Kr;  // non-equilibrium: its own reverse rate
-        if (x.rev == 1) Kr = k.Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
-        finish(r, x, k.Kf, Kr);
-    }
-    g.sync();
+    net_production<G, MT>(g, M, s, p, logP, Tc, logT, invT, pf, out);
     double cpm = 0, dtd = 0;
     for (int i = g.rank; i < ns; i += G) {
-        double w = 0;
-        const int e1 = __ldg(&M.incOff[i + 1]);
-        for (int e = __ldg(&M.incOff[i]); e < e1; e++) {
-            const int v = __ldg(&M.inc[e]);
-            const double qq = s.q[v >> 1];
-            w = (v & 1) ? w + qq : w - qq;
-        }
-        const double dY = (__ldg(&M.W[i]) * invrhoM) * w;
+        const double dY = (__ldg(&M.W[i]) * invrhoM) * out[i];
         out[i] = dY;
         cpm = fma(YT[i], s.Cp[i], cpm);
         dtd = fma(s.Ha[i], dY, dtd);
@@ -820,54 +874,10 @@ __device__ __noinline__ double rates_eval(const Grp<G>& g, const DevMech& M, con
     g.sync();
     const PFactor pf = pressure_factors(Tc);
     const double logP = M.nPlog ? log(p) : 0.0;
-    // The special block [spBegin, spBegin + nSp) of the packed order (first
-    // non-equilibrium to last fall-off reaction) runs in a loop of its own, so
-    // that the main loop carries neither the fall-off call nor a second
-    // Arrhenius.
-    auto finish = [&](const int r, const RxnInfo& x, const double Kf, const double Kr) {
-        double CF = s.C[x.sl[0]];
-        #pragma unroll 1
-        for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
-        double CR = s.C[x.sr[0]];
-        #pragma unroll 1
-        for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
-        s.q[r] = Kf * CF - Kr * CR;
-    };
-    for (int j = g.rank; j < M.nr - M.nSp; j += G) {
-        const int r = j < M.spBegin ? j : j + M.nSp;
-        const RxnInfo x = load_rx(M.rx + r);
-        double Kf;
-        if (x.kind == FCS_RXN_PLOG) {
-            double dk;
-            Kf = plog_rate(M, x.plog, p, logP, logT, invT, &dk);
-        } else if (x.tind) {
-            Kf = x.A;
-        } else {
-            Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
-        }
-        if (x.tb >= 0) Kf *= s.Mtb[x.tb];
-        double Kr = 0;
-        if (x.rev) Kr = Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
-        finish(r, x, Kf, Kr);
-    }
-    for (int r = M.spBegin + g.rank; r < M.spBegin + M.nSp; r += G) {
-        const RxnInfo x = load_rx(M.rx + r);
-        const SpecialK k = special_rates(M, x, s.Mtb, Tc, logT, invT, false);
-        double Kr = k.Kr;  // non-equilibrium: its own reverse rate
-        if (x.rev == 1) Kr = k.Kf * inv_equilibrium_kc(x, s.B, s.Binv, pf);
-        finish(r, x, k.Kf, Kr);
-    }
-    g.sync();
+    net_production<G, MT>(g, M, s, p, logP, Tc, logT, invT, pf, RR);
     double qd = 0;
     for (int i = g.rank; i < ns; i += G) {
-        double w = 0;
-        const int e1 = __ldg(&M.incOff[i + 1]);
-        for (int e = __ldg(&M.incOff[i]); e < e1; e++) {
-            const int v = __ldg(&M.inc[e]);
-            const double qq = s.q[v >> 1];
-            w = (v & 1) ? w + qq : w - qq;
-        }
-        const double rr = w * __ldg(&M.W[i]);
+        const double rr = RR[i] * __ldg(&M.W[i]);
         RR[i] = rr;
         qd -= __ldg(&M.hf[i]) * rr;
     }
@@ -937,13 +947,10 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
         s.Mtb[t] = m;
     }
     g.sync();
-    // per-reaction rate constants, their temperature derivatives and q
+    // per-reaction rate constants, their temperature derivatives and q, one
+    // chunk of reactions at a time (see net_rates_chunk)
     const PFactor pf = pressure_factors(Tc);
     const double logP = M.nPlog ? log(p) : 0.0;
-    // The special block [spBegin, spBegin + nSp) of the packed order (first
-    // non-equilibrium to last fall-off reaction) runs in a loop of its own, so
-    // that the main loop carries neither the fall-off call nor a second
-    // Arrhenius.
     // Kr, dKr/dT and dKr/dM through Kc (JF* reversible branch)
     auto through_kc = [&](const RxnInfo& x, const double Kf, const double dKfdT, const double dKfdC,
                           double& Kr, double& dKrdT, double& dKrdC) {
@@ -960,91 +967,113 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
         dKrdT = dKfdT * invKc - (invKc < inv_kc_clamp(x) ? Kr * dKcdTByKc : 0.0);
         dKrdC = dKfdC * invKc;
     };
-    auto finish = [&](const int r, const RxnInfo& x, const double Kf, const double dKfdT, const double dKfdC,
-                      const double Kr, const double dKrdT, const double dKrdC) {
-        double CF = s.C[x.sl[0]];
-        #pragma unroll 1
-        for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
-        double CR = s.C[x.sr[0]];
-        #pragma unroll 1
-        for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
-        s.Kf[r] = Kf;
-        s.Kr[r] = Kr;
-        s.q[r] = Kf * CF - Kr * CR;
-        s.dqdT[r] = dKfdT * CF - dKrdT * CR;
-        // third-body weight w = dKf/dM CF - dKr/dM CR
-        if (x.tb >= 0) s.tbF[x.tb] = dKfdC * CF - dKrdC * CR;
-    };
-    for (int j = g.rank; j < M.nr - M.nSp; j += G) {
-        const int r = j < M.spBegin ? j : j + M.nSp;
-        const RxnInfo x = load_rx(M.rx + r);
-        double Kf, dKfdT;
-        if (x.kind == FCS_RXN_PLOG) {
-            Kf = plog_rate(M, x.plog, p, logP, logT, invT, &dKfdT);
-        } else if (x.tind) {
-            Kf = x.A; dKfdT = 0;
-        } else {
-            Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
-            dKfdT = Kf * (fma(x.Ta, invT, x.beta) * invT);
-        }
-        double dKfdC = 0;
-        if (x.tb >= 0) {
-            const double Mt = s.Mtb[x.tb];
-            dKfdC = Kf;
-            Kf *= Mt;
-            dKfdT *= Mt;
-        }
-        double Kr = 0, dKrdT = 0, dKrdC = 0;
-        if (x.rev) through_kc(x, Kf, dKfdT, dKfdC, Kr, dKrdT, dKrdC);
-        finish(r, x, Kf, dKfdT, dKfdC, Kr, dKrdT, dKrdC);
-    }
-    for (int r = M.spBegin + g.rank; r < M.spBegin + M.nSp; r += G) {
-        const RxnInfo x = load_rx(M.rx + r);
-        SpecialK k = special_rates(M, x, s.Mtb, Tc, logT, invT, true);
-        // non-equilibrium: the reverse Arrhenius (JacobianFunctionI.H:129-130, Jacobian.C:412-422)
-        if (x.rev == 1) through_kc(x, k.Kf, k.dKfdT, k.dKfdC, k.Kr, k.dKrdT, k.dKrdC);
-        finish(r, x, k.Kf, k.dKfdT, k.dKfdC, k.Kr, k.dKrdT, k.dKrdC);
+    // The running sums of the rows: f[i] collects w_i (the net production),
+    // s.dCpdT[i] (free once CpM and dCpM/dT are formed) collects the
+    // temperature-column sum of dq/dT.
+    double* tcAcc = s.dCpdT;
+    for (int i = g.rank; i < ns; i += G) {
+        s.cur[i] = __ldg(&M.incOff[i]);
+        f[i] = 0.0;
+        tcAcc[i] = 0.0;
     }
     for (int idx = g.rank; idx < ns * ld; idx += G) J[idx] = MT(0);
-    g.sync();
-    // (1) column owners: d q_r / d C_j computed once per (reaction, column)
-    // occurrence and scattered down column j to the rows of reaction r, in
-    // reaction order (JF11..JF33 reverse and forward concentration terms).
-    for (int j = g.rank; j < ns; j += G) {
-        const int e1 = __ldg(&M.incOff[j + 1]);
-        for (int e = __ldg(&M.incOff[j]); e < e1; e++) {
-            const int v = __ldg(&M.inc[e]);
-            const int r = v >> 1;
-            const bool prod = v & 1;
+    const int sp0 = M.spBegin, sp1 = M.spBegin + M.nSp;
+    for (int c0 = 0; c0 < M.nr; c0 += s.rc) {
+        const int c1 = min(M.nr, c0 + s.rc);
+        auto finish = [&](const int r, const RxnInfo& x, const double Kf, const double dKfdT, const double dKfdC,
+                          const double Kr, const double dKrdT, const double dKrdC) {
+            double CF = s.C[x.sl[0]];
+            #pragma unroll 1
+            for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
+            double CR = s.C[x.sr[0]];
+            #pragma unroll 1
+            for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
+            s.Kf[r - c0] = Kf;
+            s.Kr[r - c0] = Kr;
+            s.q[r - c0] = Kf * CF - Kr * CR;
+            s.dqdT[r - c0] = dKfdT * CF - dKrdT * CR;
+            // third-body weight w = dKf/dM CF - dKr/dM CR
+            if (x.tb >= 0) s.tbF[x.tb] = dKfdC * CF - dKrdC * CR;
+        };
+        for (int r = c0 + g.rank; r < c1; r += G) {
+            if (r >= sp0 && r < sp1) continue;
             const RxnInfo x = load_rx(M.rx + r);
-            double d;
-            if (!prod) {
-                // forward: Kf * product of the other reactant concentrations
-                bool skipped = false;
-                d = s.Kf[r];
-                #pragma unroll 1
-                for (int q = 0; q < x.nl; q++) {
-                    if (!skipped && x.sl[q] == j) { skipped = true; continue; }
-                    d *= s.C[x.sl[q]];
-                }
+            double Kf, dKfdT;
+            if (x.kind == FCS_RXN_PLOG) {
+                Kf = plog_rate(M, x.plog, p, logP, logT, invT, &dKfdT);
+            } else if (x.tind) {
+                Kf = x.A; dKfdT = 0;
             } else {
-                if (!x.rev) continue;
-                bool skipped = false;
-                d = -s.Kr[r];
-                #pragma unroll 1
-                for (int q = 0; q < x.nr; q++) {
-                    if (!skipped && x.sr[q] == j) { skipped = true; continue; }
-                    d *= s.C[x.sr[q]];
-                }
+                Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
+                dKfdT = Kf * (fma(x.Ta, invT, x.beta) * invT);
             }
-            const MT md = MT(d);
-            #pragma unroll 1
-            for (int q = 0; q < x.nl; q++) { MT& c = J[(size_t)x.sl[q] * ld + j]; c = c - md; }
-            #pragma unroll 1
-            for (int q = 0; q < x.nr; q++) { MT& c = J[(size_t)x.sr[q] * ld + j]; c = c + md; }
+            double dKfdC = 0;
+            if (x.tb >= 0) {
+                const double Mt = s.Mtb[x.tb];
+                dKfdC = Kf;
+                Kf *= Mt;
+                dKfdT *= Mt;
+            }
+            double Kr = 0, dKrdT = 0, dKrdC = 0;
+            if (x.rev) through_kc(x, Kf, dKfdT, dKfdC, Kr, dKrdT, dKrdC);
+            finish(r, x, Kf, dKfdT, dKfdC, Kr, dKrdT, dKrdC);
         }
+        for (int r = max(c0, sp0) + g.rank; r < min(c1, sp1); r += G) {
+            const RxnInfo x = load_rx(M.rx + r);
+            SpecialK k = special_rates(M, x, s.Mtb, Tc, logT, invT, true);
+            // non-equilibrium: the reverse Arrhenius (JacobianFunctionI.H:129-130, Jacobian.C:412-422)
+            if (x.rev == 1) through_kc(x, k.Kf, k.dKfdT, k.dKfdC, k.Kr, k.dKrdT, k.dKrdC);
+            finish(r, x, k.Kf, k.dKfdT, k.dKfdC, k.Kr, k.dKrdT, k.dKrdC);
+        }
+        g.sync();
+        // Per species j and reaction r of the chunk (reaction order): the row
+        // sums of j (w_j, dq/dT), and as the owner of column j, d q_r / d C_j
+        // scattered down column j to the rows of reaction r (JF11..JF33
+        // reverse and forward concentration terms).
+        for (int j = g.rank; j < ns; j += G) {
+            double w = f[j], tc = tcAcc[j];
+            int e = s.cur[j];
+            const int e1 = __ldg(&M.incOff[j + 1]);
+            for (; e < e1; e++) {
+                const int v = __ldg(&M.inc[e]);
+                const int r = v >> 1;
+                if (r >= c1) break;
+                const bool prod = v & 1;
+                const double qq = s.q[r - c0], dq = s.dqdT[r - c0];
+                if (prod) { w += qq; tc += dq; } else { w -= qq; tc -= dq; }
+                const RxnInfo x = load_rx(M.rx + r);
+                double d;
+                if (!prod) {
+                    // forward: Kf * product of the other reactant concentrations
+                    bool skipped = false;
+                    d = s.Kf[r - c0];
+                    #pragma unroll 1
+                    for (int q = 0; q < x.nl; q++) {
+                        if (!skipped && x.sl[q] == j) { skipped = true; continue; }
+                        d *= s.C[x.sl[q]];
+                    }
+                } else {
+                    if (!x.rev) continue;
+                    bool skipped = false;
+                    d = -s.Kr[r - c0];
+                    #pragma unroll 1
+                    for (int q = 0; q < x.nr; q++) {
+                        if (!skipped && x.sr[q] == j) { skipped = true; continue; }
+                        d *= s.C[x.sr[q]];
+                    }
+                }
+                const MT md = MT(d);
+                #pragma unroll 1
+                for (int q = 0; q < x.nl; q++) { MT& c = J[(size_t)x.sl[q] * ld + j]; c = c - md; }
+                #pragma unroll 1
+                for (int q = 0; q < x.nr; q++) { MT& c = J[(size_t)x.sr[q] * ld + j]; c = c + md; }
+            }
+            s.cur[j] = e;
+            f[j] = w;
+            tcAcc[j] = tc;
+        }
+        g.sync();  // the next chunk overwrites Kf, Kr, q, dq/dT; the passes below read J
     }
-    g.sync();
     // (2) third-body columns, J_ij += nu_i w_t E_tj (JF* third-body block)
     for (int j = g.rank; j < ns; j += G) {
         for (int e = 0; e < M.nTbInc; e++) {
@@ -1056,19 +1085,12 @@ __device__ __noinline__ void jac_eval(const Grp<G>& g, const DevMech& M, const S
         }
     }
     g.sync();
-    // (3) row owners: production rate and temperature column by gather, then
-    // the dC/dY conversion of the row (diagonal scaling + rank-1 correction)
+    // (3) row owners: production rate, temperature column and the dC/dY
+    // conversion of the row (diagonal scaling + rank-1 correction)
     double dtd = 0, dd = 0;
     for (int i = g.rank; i < ns; i += G) {
         MT* row = J + (size_t)i * ld;
-        double w = 0, tc = 0;
-        const int e1 = __ldg(&M.incOff[i + 1]);
-        for (int e = __ldg(&M.incOff[i]); e < e1; e++) {
-            const int v = __ldg(&M.inc[e]);
-            const int r = v >> 1;
-            const double qq = s.q[r], dq = s.dqdT[r];
-            if (v & 1) { w += qq; tc += dq; } else { w -= qq; tc -= dq; }
-        }
+        const double w = f[i], tc = tcAcc[i];
         const double WiByrhoM = invRhoM * __ldg(&M.W[i]);
         const double dY = w * WiByrhoM;
         double S = 0;
