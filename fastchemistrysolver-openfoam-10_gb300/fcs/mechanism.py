@@ -315,7 +315,8 @@ def synthetic_mechanism(n_species: int, n_reactions: int, n_third_body: int,
                         n_plog: int, seed: int, n_elements: int = 3,
                         max_count: int = 3, plog_points: int = 5,
                         plog_p_range=(1e4, 1e8), hf_range_kJ=(-100.0, 100.0),
-                        name: Optional[str] = None, n_falloff=(0, 0, 0), n_noneq=(0, 0)) -> Mechanism:
+                        name: Optional[str] = None, n_falloff=(0, 0, 0), n_noneq=(0, 0),
+                        n_long=(0, 0)) -> Mechanism:
     """Build one seeded synthetic mechanism (all reactions reversible).
 
     The reactions are emitted in a shuffled *file* order so that the type
@@ -420,6 +421,33 @@ def synthetic_mechanism(n_species: int, n_reactions: int, n_third_body: int,
             eff = rng.uniform(0.5, 5.0, size=n_species) if kind == NONEQ_THIRD_BODY else None
             reactions.append(Reaction(kind, True, lr[0], lr[1], A, beta, Ta, efficiencies=eff,
                                       reverse=(math.exp(lnA_r), beta, Ta_r)))
+    # long reactions (the reference's generic RFG/JFG path, more than three
+    # species on a side): three balanced templates written as one reaction.
+    # Irreversible ones mix exchanges and dissociations (global steps of
+    # reduced mechanisms, up to 3 reactants and 7 products); reversible ones
+    # join three dissociations (3 reactants, 6 products, dnu = 3).
+    for reversible, count in ((False, n_long[0]), (True, n_long[1])):
+        for _ in range(count):
+            for _attempt in range(200):
+                lhs, rhs = [], []
+                for _k in range(3):
+                    if reversible or rng.random() < 0.6:
+                        lr = builder.recombination()
+                        if lr is not None and len(lr[0]) == 2:
+                            lr = (lr[1], lr[0])          # written as the dissociation
+                    else:
+                        lr = builder.exchange()
+                        lr = orient(lr) if lr is not None else None
+                    if lr is None:
+                        break
+                    lhs += list(lr[0])
+                    rhs += list(lr[1])
+                if lr is not None and len(lhs) <= 4 and 3 < len(rhs) <= 8:
+                    break
+            else:
+                raise RuntimeError("could not close a long template; change the seed")
+            A, beta, Ta = _arrhenius(rng)
+            reactions.append(Reaction(ARRHENIUS, reversible, sorted(lhs), sorted(rhs), A, beta, Ta))
     while len(reactions) < n_reactions:
         r = rng.random()
         lr = builder.exchange() if r < 0.8 else builder.recombination()

@@ -26,6 +26,10 @@ Workloads (all seeds fixed):
   3 non-equilibrium third-body, 2 third-body, 1 PLOG, 1 Lindemann, 1 Troe),
   512 cells drawn like ``falloff_16s``: the parity case of the
   non-equilibrium kinds.
+* ``long_24s`` -- 24 species / 60 reactions, among them 4 irreversible global
+  reactions (up to 3 reactants and 7 products) and 2 reversible ones with 6
+  products (dnu = 3), plus one of each other kind; 512 cells drawn like
+  ``falloff_16s``: the parity case of the long reactions.
 * ``large_200s`` -- 200 species / 1,500 reactions (60 PLOG, 40 third-body),
   1,048,576 cells, T ~ U[600, 2400] K, p ~ U[1e5, 4e6] Pa, Y ~ Dirichlet(0.2),
   dt = 1e-5 s.
@@ -107,6 +111,11 @@ WORKLOADS = {
         dict(n_species=14, n_reactions=40, n_third_body=2, n_plog=1, seed=1414, n_falloff=(1, 1, 0),
              n_noneq=(6, 3)),
         n_cells=512, dt=1e-5, cell_seed=14),
+    "long_24s": Workload(
+        "long_24s",
+        dict(n_species=24, n_reactions=60, n_third_body=2, n_plog=1, seed=2426, n_falloff=(1, 0, 1),
+             n_noneq=(1, 1), n_long=(4, 2)),
+        n_cells=512, dt=1e-5, cell_seed=24),
     "large_200s": Workload(
         "large_200s",
         dict(n_species=200, n_reactions=1500, n_third_body=40, n_plog=60, seed=2000),
@@ -147,7 +156,7 @@ def cells_for(w: Workload, mech: Mechanism, n: Optional[int] = None,
                               rng.uniform(1200.0, 2200.0, n_full)))
         p = rng.uniform(1e5, 1e6, n_full)
         Y = rng.dirichlet(np.full(ns, 0.3), size=n_full).T
-    elif w.name in ("falloff_16s", "noneq_14s"):
+    elif w.name in ("falloff_16s", "noneq_14s", "long_24s"):
         T = rng.uniform(900.0, 1800.0, n_full)
         p = 10.0 ** rng.uniform(4.0, 7.0, n_full)
         Y = rng.dirichlet(np.full(ns, 0.5), size=n_full).T

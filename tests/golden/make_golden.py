@@ -37,6 +37,7 @@ CASES = [
     ("falloff_16s", 32, "OptSeulex"),
     ("noneq_14s", 64, "OptRodas34"),
     ("noneq_14s", 32, "OptSeulex"),
+    ("long_24s", 64, "OptRodas34"),
 ]
 
 
@@ -72,6 +73,7 @@ TC = [
     ("uneven_111s", 64),
     ("falloff_16s", 64),
     ("noneq_14s", 64),
+    ("long_24s", 64),
 ]
 
 

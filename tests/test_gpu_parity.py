@@ -63,7 +63,8 @@ def test_exp_against_cuda(built):
 
 
 @pytest.mark.parametrize("wname,n", [("ignition_10s", 64), ("counterflow_53s", 32), ("uneven_111s", 16),
-                                     ("large_200s", 4), ("falloff_16s", 64), ("noneq_14s", 64)])
+                                     ("large_200s", 4), ("falloff_16s", 64), ("noneq_14s", 64),
+                                     ("long_24s", 64)])
 def test_rhs_and_jacobian_match_oracle(built, wname, n):
     import oracle
     w, mech, flat, c = _setup(wname, n)
@@ -96,7 +97,7 @@ GOLDEN_CASES = ["ignition_10s_OptRodas34", "ignition_10s_OptRosenbrock34", "igni
                 "ignition_10s_OptRodas23", "ignition_10s_OptRosenbrock23",
                 "counterflow_53s_OptRodas23", "counterflow_53s_OptRosenbrock23",
                 "falloff_16s_OptRodas34", "falloff_16s_OptSeulex",
-                "noneq_14s_OptRodas34", "noneq_14s_OptSeulex"]
+                "noneq_14s_OptRodas34", "noneq_14s_OptSeulex", "long_24s_OptRodas34"]
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
@@ -264,7 +265,7 @@ def test_strided_host_inputs(built):
     np.testing.assert_array_equal(ctx.rates(p, T, rho, Y)[0], ctx.rates(pc, Tc, rc, Yc)[0])
 
 
-@pytest.mark.parametrize("wname", ["counterflow_53s", "falloff_16s", "noneq_14s"])
+@pytest.mark.parametrize("wname", ["counterflow_53s", "falloff_16s", "noneq_14s", "long_24s"])
 def test_mechanism_from_openfoam_files(built, tmp_path, wname):
     """Loading the OpenFOAM reactions / speciesThermo dictionaries gives the
     same chemistry as the flat description: PLOG ArrheniusData, third-body
@@ -321,7 +322,7 @@ def test_queue_order_and_graph_replay_do_not_change_results(built):
             assert s[k] == s0[k], k
 
 
-@pytest.mark.parametrize("wname", ["ignition_10s", "counterflow_53s", "uneven_111s", "falloff_16s", "noneq_14s"])
+@pytest.mark.parametrize("wname", ["ignition_10s", "counterflow_53s", "uneven_111s", "falloff_16s", "noneq_14s", "long_24s"])
 def test_tc_matches_reference_golden(built, wname):
     """fcs_tc against FastChemistryModel::tc() of the reference
     (tests/golden/tc.npz); differences are summation order and exp rounding."""

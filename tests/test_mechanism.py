@@ -14,7 +14,8 @@ def test_generator_sizes_and_balance(name):
     assert m.n_species == a["n_species"] and m.n_reactions == a["n_reactions"]
     assert m.count(THIRD_BODY) == a["n_third_body"] and m.count(PLOG) == a["n_plog"]
     for r in m.reactions:
-        assert 1 <= len(r.lhs) <= 3 and 1 <= len(r.rhs) <= 3
+        long = a.get("n_long", (0, 0))
+        assert 1 <= len(r.lhs) <= (4 if sum(long) else 3) and 1 <= len(r.rhs) <= (8 if sum(long) else 3)
         # atom conservation by construction
         assert np.array_equal(m.composition[r.lhs].sum(0), m.composition[r.rhs].sum(0))
         if r.kinf is not None:

@@ -21,7 +21,7 @@ CASES = ["ignition_10s_OptRodas34", "ignition_10s_OptRosenbrock34", "ignition_10
          "ignition_10s_OptRodas23", "ignition_10s_OptRosenbrock23",
          "counterflow_53s_OptRodas23", "counterflow_53s_OptRosenbrock23",
          "falloff_16s_OptRodas34", "falloff_16s_OptSeulex",
-         "noneq_14s_OptRodas34", "noneq_14s_OptSeulex"]
+         "noneq_14s_OptRodas34", "noneq_14s_OptSeulex", "long_24s_OptRodas34"]
 
 
 def _setup(case):
@@ -64,7 +64,7 @@ def test_port_matches_reference_integration(case, port_built):
 
 
 @pytest.mark.parametrize("case", ["ignition_10s_OptRodas34", "counterflow_53s_OptRodas34", "falloff_16s_OptRodas34",
-                                  "noneq_14s_OptRodas34"])
+                                  "noneq_14s_OptRodas34", "long_24s_OptRodas34"])
 def test_port_matches_reference_rhs_and_jacobian(case, port_built):
     import oracle
     w, flat, solver, g, cells = _setup(case)
@@ -124,7 +124,7 @@ def test_port_against_compiled_reference_directly(port_built):
     np.testing.assert_allclose(r1["Y"], r0["Y"], atol=1e-9)
 
 
-@pytest.mark.parametrize("wname", ["ignition_10s", "counterflow_53s", "uneven_111s", "falloff_16s", "noneq_14s"])
+@pytest.mark.parametrize("wname", ["ignition_10s", "counterflow_53s", "uneven_111s", "falloff_16s", "noneq_14s", "long_24s"])
 def test_port_tc_matches_reference_golden(wname, port_built):
     """FastChemistryModel::tc() of the reference (tests/golden/tc.npz)."""
     import oracle
