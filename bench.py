@@ -169,11 +169,27 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(flat, w, cells, seconds, threads):
-    """The oracle restatement of the reference CPU integrator on a bounded
-    sample of the workload's cells (all host threads)."""
+PORT_NOTE = ("oracle port (scalar C restatement): the reference core needs x86 AVX2 and glibc libmvec and "
+             "does not build on this host; per core it is slower than the reference's vectorised core")
+
+
+def cpu_integrator(flat, w):
+    """The reference's own core (compiled from its sources) where it is built
+    on this host, else the oracle port.  Returns (integrate(cells, threads), kind)."""
     import oracle
+    if os.path.exists(oracle.REF_SO):
+        ref = oracle.Reference(flat, solver=w.solver, abs_tol=w.abs_tol, rel_tol=w.rel_tol)
+        return (lambda sub, threads: ref.integrate(sub, w.dt, treact=w.treact, threads=threads)), "reference"
     port = oracle.Port(flat)
+    return (lambda sub, threads: port.integrate(sub, w.dt, solver=w.solver, abs_tol=w.abs_tol, rel_tol=w.rel_tol,
+                                                treact=w.treact, threads=threads)), "port"
+
+
+def cpu_baseline(flat, w, cells, seconds, threads):
+    """The reference CPU integrator (its own core, else the oracle port) on a
+    bounded sample of the workload's cells (all host threads).  Returns
+    (cells/s, cells done, seconds, kind)."""
+    run, kind = cpu_integrator(flat, w)
     rng = np.random.default_rng(7)
     order = rng.permutation(cells.n)
     n = max(threads * 2, 32)
@@ -182,8 +198,7 @@ def cpu_baseline(flat, w, cells, seconds, threads):
     while True:
         sub = cells.subset(order[done:done + n])
         t0 = time.perf_counter()
-        port.integrate(sub, w.dt, solver=w.solver, abs_tol=w.abs_tol, rel_tol=w.rel_tol,
-                       treact=w.treact, threads=threads)
+        run(sub, threads)
         dt = time.perf_counter() - t0
         t_used += dt
         done += sub.n
@@ -193,7 +208,7 @@ def cpu_baseline(flat, w, cells, seconds, threads):
         n = int(min(cells.n - done, max(threads, rate * (seconds - t_used))))
         if n <= 0:
             break
-    return done / t_used, done, t_used
+    return done / t_used, done, t_used, kind
 
 
 def reference_arm(args):
@@ -205,15 +220,15 @@ def reference_arm(args):
     mech = w.mechanism()
     flat = fcs.flatten(mech)
     import oracle
-    oracle.build(ref=False)
+    oracle.build(ref=True)  # the reference core only where its sources are present (x86-64)
     cells = fcs.cells_for(w, mech, n=args.cells or None)
     threads = os.cpu_count() or 1
     per_step = max(2.0, args.cpu_seconds / max(1, args.steps))
     for _ in range(max(0, min(args.warmup, 1))):
         cpu_baseline(flat, w, cells.subset(np.arange(min(cells.n, threads))), 0.1, threads)
-    rates, total = [], 0
+    rates, total, kind = [], 0, "port"
     for _ in range(args.steps):
-        r, n, _t = cpu_baseline(flat, w, cells, per_step, threads)
+        r, n, _t, kind = cpu_baseline(flat, w, cells, per_step, threads)
         rates.append(r)
         total += n
     value = statistics.median(rates)
@@ -224,9 +239,11 @@ def reference_arm(args):
             "data": "synthetic (seeded)",
             "config": {"workload": w.name, "cells": cells.n, "solver": w.solver, "precision": "fp64",
                        "dt": w.dt, "abs_tol": w.abs_tol, "rel_tol": w.rel_tol},
-            "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": "port",
+            "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": kind,
                              "sample": sample},
             "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if kind == "port":
+        line["cpu_baseline"]["note"] = PORT_NOTE
     print(json.dumps(line), flush=True)
 
 
@@ -490,9 +507,11 @@ def main():
         line["accuracy"] = acc
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        rate, done, tu = cpu_baseline(flat, w, cells, args.cpu_seconds, threads)
-        line["cpu_baseline"] = {"value": rate, "unit": "cells/s", "cores": threads, "kind": "port",
+        rate, done, tu, kind = cpu_baseline(flat, w, cells, args.cpu_seconds, threads)
+        line["cpu_baseline"] = {"value": rate, "unit": "cells/s", "cores": threads, "kind": kind,
                                 "sample": f"{done} randomly chosen cells of the same field, {tu:.1f} s of CPU time"}
+        if kind == "port":
+            line["cpu_baseline"]["note"] = PORT_NOTE
     print(json.dumps(line), flush=True)
 
 
