@@ -83,9 +83,11 @@ enum { FCS_SOLVER_RODAS34 = 0, FCS_SOLVER_ROSENBROCK34 = 1, FCS_SOLVER_SEULEX = 
        FCS_SOLVER_RODAS23 = 3,        /* src/ODE/OptRodas23/OptRodas23.C:202-315       */
        FCS_SOLVER_ROSENBROCK23 = 4 }; /* src/ODE/OptRosenbrock23/OptRosenbrock23.C:208-298 */
 enum { FCS_JACOBIAN_EXACT = 0, FCS_JACOBIAN_FAST = 1 };
-/* FCS_PRECISION_MIXED: Jacobian storage and LU in FP32, one FP64-residual
- * iterative-refinement sweep per linear solve; rates, thermo, equilibrium
- * constants, state and the step controller stay FP64. */
+/* FCS_PRECISION_MIXED: the iteration matrix factored in FP32 (power-of-two
+ * row and column equilibration), one FP64-residual refinement sweep per
+ * linear solve against the FP64 Jacobian; an attempt whose correction is not
+ * small is redone in FP64.  Rates, thermo, equilibrium constants, the
+ * Jacobian assembly, state and the step controller stay FP64. */
 enum { FCS_PRECISION_FP64 = 0, FCS_PRECISION_MIXED = 1 };
 /* Cell-to-thread mapping: AUTO lets the autotuner choose. */
 enum { FCS_MAPPING_AUTO = 0, FCS_MAPPING_WARP = 32, FCS_MAPPING_BLOCK64 = 64,
