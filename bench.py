@@ -185,21 +185,24 @@ def cpu_integrator(flat, w):
                                                 treact=w.treact, threads=threads)), "port"
 
 
-def cpu_baseline(flat, w, cells, seconds, threads):
+def cpu_baseline(flat, w, cells, seconds, threads, stats=None):
     """The reference CPU integrator (its own core, else the oracle port) on a
     bounded sample of the workload's cells (all host threads).  Returns
-    (cells/s, cells done, seconds, kind)."""
+    (cells/s, cells done, seconds, kind); `stats` (a dict) also gets the
+    attempts per cell (Jacobians per cell: one per Rosenbrock attempt)."""
     run, kind = cpu_integrator(flat, w)
     rng = np.random.default_rng(7)
     order = rng.permutation(cells.n)
     n = max(threads * 2, 32)
     t_used = 0.0
     done = 0
+    jac = 0
     while True:
         sub = cells.subset(order[done:done + n])
         t0 = time.perf_counter()
-        run(sub, threads)
+        out = run(sub, threads)
         dt = time.perf_counter() - t0
+        jac += int(out["counters"]["jacobians"])
         t_used += dt
         done += sub.n
         if t_used >= seconds or done >= cells.n:
@@ -208,7 +211,24 @@ def cpu_baseline(flat, w, cells, seconds, threads):
         n = int(min(cells.n - done, max(threads, rate * (seconds - t_used))))
         if n <= 0:
             break
+    if stats is not None:
+        stats["jacobians_per_cell"] = jac / max(1, done)
     return done / t_used, done, t_used, kind
+
+
+def cpu_single_core(flat, w, cells, seconds):
+    """One host thread on a few cells of the same sample order: cells/s."""
+    run, _ = cpu_integrator(flat, w)
+    order = np.random.default_rng(7).permutation(cells.n)
+    done, t_used, n = 0, 0.0, 2
+    while t_used < seconds and done < cells.n:
+        sub = cells.subset(order[done:done + n])
+        t0 = time.perf_counter()
+        run(sub, 1)
+        t_used += time.perf_counter() - t0
+        done += sub.n
+        n = max(1, min(cells.n - done, int(done / t_used * max(0.5, seconds - t_used)) + 1))
+    return done / t_used
 
 
 def reference_arm(args):
@@ -226,9 +246,9 @@ def reference_arm(args):
     per_step = max(2.0, args.cpu_seconds / max(1, args.steps))
     for _ in range(max(0, min(args.warmup, 1))):
         cpu_baseline(flat, w, cells.subset(np.arange(min(cells.n, threads))), 0.1, threads)
-    rates, total, kind = [], 0, "port"
+    rates, total, kind, extra = [], 0, "port", {}
     for _ in range(args.steps):
-        r, n, _t, kind = cpu_baseline(flat, w, cells, per_step, threads)
+        r, n, _t, kind = cpu_baseline(flat, w, cells, per_step, threads, extra)
         rates.append(r)
         total += n
     value = statistics.median(rates)
@@ -240,7 +260,8 @@ def reference_arm(args):
             "config": {"workload": w.name, "cells": cells.n, "solver": w.solver, "precision": "fp64",
                        "dt": w.dt, "abs_tol": w.abs_tol, "rel_tol": w.rel_tol},
             "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": kind,
-                             "sample": sample},
+                             "sample": sample, "jacobians_per_cell": extra.get("jacobians_per_cell"),
+                             "single_core": cpu_single_core(flat, w, cells, min(5.0, per_step / 2))},
             "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if kind == "port":
         line["cpu_baseline"]["note"] = PORT_NOTE
@@ -507,9 +528,12 @@ def main():
         line["accuracy"] = acc
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        rate, done, tu, kind = cpu_baseline(flat, w, cells, args.cpu_seconds, threads)
+        extra = {}
+        rate, done, tu, kind = cpu_baseline(flat, w, cells, args.cpu_seconds, threads, extra)
         line["cpu_baseline"] = {"value": rate, "unit": "cells/s", "cores": threads, "kind": kind,
-                                "sample": f"{done} randomly chosen cells of the same field, {tu:.1f} s of CPU time"}
+                                "sample": f"{done} randomly chosen cells of the same field, {tu:.1f} s of CPU time",
+                                "jacobians_per_cell": extra["jacobians_per_cell"],
+                                "single_core": cpu_single_core(flat, w, cells, min(5.0, args.cpu_seconds / 3))}
         if kind == "port":
             line["cpu_baseline"]["note"] = PORT_NOTE
     print(json.dumps(line), flush=True)
