@@ -333,30 +333,46 @@ bool fcs::make_shape(fcs_ctx* ctx, int group, bool integrate, Shape& sh) {
     const bool mixed = o.precision == FCS_PRECISION_MIXED;
     const bool seulex = integrate && o.solver == FCS_SOLVER_SEULEX;
     sh.mixed = mixed;
-    sh.L = make_layout(ctx->M.ns, ctx->M.nr, ctx->M.nTB, mixed, seulex, group);
     sh.lc.group = group;
     if (ctx->M.n > 256) return false;  // the solves keep <= 256 unknowns per warp lane set
     const size_t smemCap = ctx->maxSmemPerBlock;
-    int groupsPerBlock = 1;
-    if (group == 32) {
-        groupsPerBlock = (int)std::min<size_t>(8, smemCap / (size_t)sh.L.bytes);
-        if (groupsPerBlock < 1) groupsPerBlock = 1;
-    }
-    sh.global = (size_t)sh.L.bytes > smemCap;
-    sh.lc.block = group * groupsPerBlock;
     int maxThreads = 0, regs = 0;
     if (integrate_attributes(group, mixed, &maxThreads, &regs) != cudaSuccess) return false;
-    if (sh.lc.block > maxThreads) return false;
-    // resident blocks per SM: shared memory and registers
-    int perSM = 1;
-    if (!sh.global) {
-        const size_t perBlock = (size_t)sh.L.bytes * groupsPerBlock + 1024;
-        perSM = (int)std::max<size_t>(1, (228 * 1024) / perBlock);
-    } else {
-        perSM = 2;
+    // Cells resident per SM for a layout: groups per block (group 32 packs up
+    // to 8 cells into a block), blocks per SM by shared memory and registers.
+    struct Res { int gpb, perSM; bool global; int cells; };
+    auto residency = [&](const SlotLayout& L) {
+        Res r;
+        r.gpb = 1;
+        if (group == 32) r.gpb = (int)std::max<size_t>(1, std::min<size_t>(8, smemCap / (size_t)L.bytes));
+        r.global = (size_t)L.bytes > smemCap;
+        const int block = group * r.gpb;
+        const int bySmem = r.global ? 2 : (int)std::max<size_t>(1, (228 * 1024) / ((size_t)L.bytes * r.gpb + 1024));
+        const int byRegs = std::max(1, 65536 / std::max(1, regs * block));
+        r.perSM = std::max(1, std::min(bySmem, byRegs));
+        r.cells = r.gpb * r.perSM;
+        return r;
+    };
+    // One chunk of reactions unless smaller chunks let more cells reside;
+    // then the largest chunk (a multiple of the group size) that does.
+    const int nr = std::max(1, ctx->M.nr);
+    auto layout = [&](int rc) { return make_layout(ctx->M.ns, ctx->M.nr, ctx->M.nTB, mixed, seulex, rc); };
+    sh.L = layout(nr);
+    Res res = residency(sh.L);
+    if (!res.global && nr > group) {
+        const Res best = residency(layout(group));
+        if (!best.global && best.cells > res.cells) {
+            for (int rc = ((nr - 1) / group) * group; rc >= group; rc -= group) {
+                const SlotLayout L = layout(rc);
+                const Res r = residency(L);
+                if (r.cells == best.cells) { sh.L = L; res = r; break; }
+            }
+        }
     }
-    const int regLimit = std::max(1, 65536 / std::max(1, regs * sh.lc.block));
-    perSM = std::max(1, std::min(perSM, regLimit));
+    sh.global = res.global;
+    sh.lc.block = group * res.gpb;
+    if (sh.lc.block > maxThreads) return false;
+    const int perSM = res.perSM;
     sh.lc.grid = ctx->numSMs * perSM;
     return true;
 }

@@ -155,7 +155,7 @@ struct SlotLayout {
     int offScale;      // row / column equilibration factors [2n] double (mixed precision)
     int offPiv;        // [n] int
     int offRx;         // Kf, Kr, q, dqdT [rc] each: one chunk of reactions
-    int rc;            // reactions per chunk (2 G, at most nr)
+    int rc;            // reactions per chunk (at most nr)
     int offCur;        // [ns] int: per-species incidence cursor across chunks
     int offTb;         // M, dKfdC, dKrdC, CF, CR [nTB] each
     int offTable;      // Seulex extrapolation table [12][n] doubles
@@ -173,7 +173,9 @@ __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 //   mixed Rosenbrock: FP32 Jacobian + FP32 LU; the FP64 view (Jacobian assembly in
 //                     FP64, and the FP64 fallback attempt) overlays both
 //   mixed Seulex    : as FP64 Seulex, with the two FP32 matrices inside the FP64 Jacobian
-__host__ __device__ inline SlotLayout make_layout(int ns, int nr, int nTB, bool mixed, bool seulex, int group) {
+// rc: reactions per chunk (clamped to [1, nr]); the host picks it so that the
+// chunks are no smaller than needed for the most cells per SM.
+__host__ __device__ inline SlotLayout make_layout(int ns, int nr, int nTB, bool mixed, bool seulex, int rc) {
     SlotLayout L;
     const int n = ns + 1;
     L.ld = n | 1;
@@ -191,7 +193,7 @@ __host__ __device__ inline SlotLayout make_layout(int ns, int nr, int nTB, bool 
     L.offInvD = o;  o = align16(o + n * 8);
     L.offScale = o; if (mixed) o = align16(o + 2 * n * 8);
     L.offPiv = o;   o = align16(o + n * 4);
-    L.rc = nr < 2 * group ? (nr > 0 ? nr : 1) : 2 * group;
+    L.rc = rc < 1 ? 1 : (nr > 0 && rc > nr ? nr : rc);
     L.offRx = o;    o = align16(o + 4 * L.rc * 8);
     L.offCur = o;   o = align16(o + ns * 4);
     L.offTb = o;    o = align16(o + 5 * (nTB > 0 ? nTB : 1) * 8);
@@ -612,9 +614,9 @@ static __device__ __forceinline__ SpecialK special_rates(const DevMech& M, const
 }
 
 // ------------------------------------------------------------------------
-// Reactions are evaluated in chunks of s.rc (2 G) so that the per-reaction
-// arrays of a cell slot hold one chunk, not the whole mechanism: the slot
-// then fits more cells per SM.  Every sum keeps its order: a species' terms
+// Reactions are evaluated in chunks of s.rc so that the per-reaction arrays
+// of a cell slot hold one chunk, not the whole mechanism, where that lets
+// more cells reside per SM (otherwise one chunk holds every reaction).  Every sum keeps its order: a species' terms
 // are added in reaction order across the chunks, its incidence cursor
 // (s.cur) carrying over from one chunk to the next.
 

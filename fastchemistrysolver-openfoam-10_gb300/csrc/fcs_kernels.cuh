@@ -957,11 +957,13 @@ inline cudaError_t launch_integrate_t(const LaunchCfg& lc, const DevMech& M, con
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
     }
-    // all of the unified L1/shared memory as shared memory: the cell slots set
-    // how many groups are resident per SM, the mechanism data reads go to L2
+    // Slots in shared memory: all of the unified L1/shared memory as shared
+    // memory (the slots set how many groups reside per SM).  Slots in the
+    // global workspace: all of it as L1, which then caches the slots.
     {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                             (int)cudaSharedmemCarveoutMaxShared);
+                                             gws ? (int)cudaSharedmemCarveoutMaxL1
+                                                 : (int)cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) return e;
     }
     k<<<lc.grid, lc.block, sm, st>>>(M, o, L, io, q, gws);
