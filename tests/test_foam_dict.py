@@ -41,3 +41,82 @@ def test_every_registered_solver_name(tmp_path, lib_path, solver, code):
     foam_io.write_chemistry_properties(path, solver=solver)
     o, _ = _lib.read_chemistry_properties(path)
     assert o.solver == code
+
+
+@pytest.mark.parametrize("wname", ["ignition_10s", "counterflow_53s", "falloff_16s", "noneq_14s", "long_24s"])
+def test_reactions_file_round_trip(tmp_path, lib_path, wname):
+    """The writer's reactions / speciesThermo files read back by the library's
+    reader (fcs_parse_mechanism_foam, no GPU) give the generator's mechanism:
+    kinds, reversibility, stoichiometry (as multisets: the file groups repeated
+    species as "2H"), Arrhenius / kInf / reverse rates, efficiencies of the
+    third-body kinds, fall-off parameters, PLOG tables and thermo."""
+    import numpy as np
+    import fcs
+    from fcs.mechanism import FALLOFF_KINDS, NONEQ_THIRD_BODY, THIRD_BODY
+    mech = fcs.WORKLOADS[wname].mechanism()
+    a = fcs.flatten(mech)
+    paths = foam_io.write_case(mech, str(tmp_path))
+    b, names = _lib.parse_mechanism_foam(paths["reactions"], paths["thermo"])
+    assert names == list(mech.species)
+    assert (b.n_species, b.n_reactions) == (a.n_species, a.n_reactions)
+    for k in ("W", "T_low", "T_high", "T_common", "high_coeffs", "low_coeffs", "type", "reversible",
+              "lhs_offset", "rhs_offset", "arrhenius", "arrhenius2", "falloff_params", "plog_offset"):
+        np.testing.assert_array_equal(getattr(b, k), getattr(a, k), err_msg=k)
+    np.testing.assert_array_equal(b.plog_table[:a.plog_table.size], a.plog_table)
+    ns = a.n_species
+    for r in range(a.n_reactions):
+        for off, sp in (("lhs_offset", "lhs_species"), ("rhs_offset", "rhs_species")):
+            o = getattr(a, off)
+            assert sorted(getattr(b, sp)[o[r]:o[r + 1]]) == sorted(getattr(a, sp)[o[r]:o[r + 1]])
+        if a.type[r] in (THIRD_BODY, NONEQ_THIRD_BODY) or a.type[r] in FALLOFF_KINDS:
+            np.testing.assert_array_equal(b.efficiencies[r * ns:(r + 1) * ns], a.efficiencies[r * ns:(r + 1) * ns])
+
+
+def test_reader_openfoam_word_and_list_forms(tmp_path, lib_path):
+    """Species names with parentheses (CH2(S)), a thermo database holding
+    species the mechanism does not use, uniform lists `7 { 0 }`, comments
+    and an entry commented out with /* */ are read as OpenFOAM reads them."""
+    import numpy as np
+    coeffs = "( 3.5 0.001 0 0 0 -1000 3 )"
+    thermo = ["species 3 ( CH2(S) CH2 H2 );"]
+    for sp, w in (("CH2(S)", 14.027), ("UNUSED", 10.0), ("CH2", 14.027), ("H2", 2.016)):
+        body = "highCpCoeffs 7 { 0 }; lowCpCoeffs 7 { 0 };" if sp == "UNUSED" else \
+            f"highCpCoeffs {coeffs}; lowCpCoeffs {coeffs};"
+        thermo.append(f"{sp} {{ specie {{ molWeight {w}; }} thermodynamics {{ Tlow 200; Thigh 3500; "
+                      f"Tcommon 1000; {body} }} }}")
+    (tmp_path / "thermo").write_text("\n".join(thermo) + "\n")
+    (tmp_path / "reactions").write_text("""// the singlet methylene quench
+reactions
+{
+    un-named-reaction-0
+    {
+        type            reversibleArrhenius;
+        reaction        "CH2(S) + H2 = CH2 + H2";   // collision partner on both sides
+        A               7e+09;
+        beta            0;
+        Ta              0;
+    }
+    /*un-named-reaction-1
+    {
+        type            irreversibleArrhenius;
+        reaction        "CH2 = CH2(S)";
+        A 1; beta 0; Ta 0;
+    }*/
+    un-named-reaction-1
+    {
+        type            irreversibleArrhenius;
+        reaction        "2CH2(S) = CH2 + CH2";
+        A               1e+10;
+        beta            0.5;
+        Ta              100;
+    }
+}
+""")
+    b, names = _lib.parse_mechanism_foam(str(tmp_path / "reactions"), str(tmp_path / "thermo"))
+    assert names == ["CH2(S)", "CH2", "H2"]
+    assert b.n_reactions == 2
+    np.testing.assert_array_equal(b.reversible, [1, 0])
+    np.testing.assert_array_equal(b.lhs_species, [0, 2, 0, 0])
+    np.testing.assert_array_equal(b.rhs_species, [1, 2, 1, 1])
+    np.testing.assert_array_equal(b.arrhenius, [7e9, 0, 0, 1e10, 0.5, 100])
+    np.testing.assert_allclose(b.W, [14.027, 14.027, 2.016])
