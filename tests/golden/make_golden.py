@@ -38,6 +38,10 @@ CASES = [
     ("noneq_14s", 64, "OptRodas34"),
     ("noneq_14s", 32, "OptSeulex"),
     ("long_24s", 64, "OptRodas34"),
+    ("falloff_16s", 32, "OptRosenbrock34"),
+    ("falloff_16s", 32, "OptRodas23"),
+    ("noneq_14s", 32, "OptRosenbrock23"),
+    ("long_24s", 32, "OptSeulex"),
 ]
 
 

@@ -97,7 +97,8 @@ GOLDEN_CASES = ["ignition_10s_OptRodas34", "ignition_10s_OptRosenbrock34", "igni
                 "ignition_10s_OptRodas23", "ignition_10s_OptRosenbrock23",
                 "counterflow_53s_OptRodas23", "counterflow_53s_OptRosenbrock23",
                 "falloff_16s_OptRodas34", "falloff_16s_OptSeulex",
-                "noneq_14s_OptRodas34", "noneq_14s_OptSeulex", "long_24s_OptRodas34"]
+                "noneq_14s_OptRodas34", "noneq_14s_OptSeulex", "long_24s_OptRodas34",
+                "falloff_16s_OptRosenbrock34", "falloff_16s_OptRodas23", "noneq_14s_OptRosenbrock23", "long_24s_OptSeulex"]
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
