@@ -60,3 +60,26 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--gpus", "2"])
     bench.main()
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_line(monkeypatch, capsys):
+    """Rank 0 of the reference arm prints one JSON line with the contract's
+    keys: the CPU integrator (the reference core where it is built, else the
+    oracle port, then with a note) on a bounded sample of the headline field."""
+    import json
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.delenv("RANK", raising=False)
+    monkeypatch.delenv("WORLD_SIZE", raising=False)
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "1", "--warmup", "1",
+                                      "--cpu-seconds", "1"])
+    bench.main()
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "cells/s" and line["higher_is_better"] is True
+    assert line["value"] > 0 and line["e2e"]["value"] == line["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    cb = line["cpu_baseline"]
+    assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["value"] == line["value"]
+    assert cb["jacobians_per_cell"] > 1 and cb["single_core"] > 0
+    assert (cb["kind"] == "port") == ("note" in cb)
+    assert line["config"]["workload"] == "counterflow_53s"
