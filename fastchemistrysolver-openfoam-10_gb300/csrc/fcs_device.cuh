@@ -157,7 +157,7 @@ struct SlotLayout {
     int offRx;         // Kf, Kr, q, dqdT [rc] each: one chunk of reactions
     int rc;            // reactions per chunk (at most nr)
     int offCur;        // [ns] int: per-species incidence cursor across chunks
-    int offTb;         // M, dKfdC, dKrdC, CF, CR [nTB] each
+    int offTb;         // M (third-body concentration), third-body column weight [nTB] each
     int offTable;      // Seulex extrapolation table [12][n] doubles
     int offRed;        // 48 doubles of reduction / broadcast scratch
     int bytes;         // total, multiple of 16
@@ -196,7 +196,7 @@ __host__ __device__ inline SlotLayout make_layout(int ns, int nr, int nTB, bool 
     L.rc = rc < 1 ? 1 : (nr > 0 && rc > nr ? nr : rc);
     L.offRx = o;    o = align16(o + 4 * L.rc * 8);
     L.offCur = o;   o = align16(o + ns * 4);
-    L.offTb = o;    o = align16(o + 5 * (nTB > 0 ? nTB : 1) * 8);
+    L.offTb = o;    o = align16(o + 2 * (nTB > 0 ? nTB : 1) * 8);
     L.offTable = o;
     if (seulex) o = align16(o + 12 * n * 8);
     L.offRed = o;   o = align16(o + 48 * 8);
@@ -219,7 +219,7 @@ struct Slot {
     double *Kf, *Kr, *q, *dqdT;   // one chunk of reactions: index r - c0
     int rc;                        // reactions per chunk
     int* cur;                      // per-species incidence cursor
-    double *Mtb, *tbF, *tbR, *tbCF, *tbCR;
+    double *Mtb, *tbF;
     double* table;
     double* red;
     __device__ double* v(int k) const { return vec + k * n; }
@@ -253,7 +253,7 @@ __device__ __forceinline__ Slot<MT> make_slot(char* base, const SlotLayout& L, c
     s.cur = reinterpret_cast<int*>(base + L.offCur);
     double* tb = reinterpret_cast<double*>(base + L.offTb);
     const int nt = M.nTB > 0 ? M.nTB : 1;
-    s.Mtb = tb; s.tbF = tb + nt; s.tbR = tb + 2 * nt; s.tbCF = tb + 3 * nt; s.tbCR = tb + 4 * nt;
+    s.Mtb = tb; s.tbF = tb + nt;
     s.table = reinterpret_cast<double*>(base + L.offTable);
     s.red = reinterpret_cast<double*>(base + L.offRed);
     return s;
