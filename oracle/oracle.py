@@ -4,8 +4,10 @@
   portable, used by tests, ``smoke()`` and the cpu_baseline / reference leg of
   ``bench.py`` as the checker and as the timed CPU baseline.
 * :class:`Reference` -- the reference's own numerical core compiled from its
-  unmodified sources (``oracle/_ref/libfcs_ref.so``, x86-64 only), used here to
-  validate the restatement and to generate the golden fixtures.
+  unmodified sources (``oracle/_ref/libfcs_ref.so``: with AVX2 on x86-64, with
+  the portable SIMD shim of ``oracle/simd_shim`` elsewhere), used to validate
+  the restatement, to generate the golden fixtures, and as the timed CPU
+  baseline of the bench where it is built.
 """
 from __future__ import annotations
 
@@ -18,8 +20,28 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libfcs_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libfcs_ref.so")
-REF_SRC = "/root/reference/src"
-REF_TUTORIAL = os.path.join(os.path.dirname(REF_SRC), "tutorial")  # mechanisms + cases
+REF_SHIM_SO = os.path.join(HERE, "_ref", "libfcs_ref_shim.so")
+STAGED_SRC = os.path.join(HERE, "_ref", "src")   # unmodified reference sources for hosts without the tree
+# Where the reference project lives is never assumed: it comes from the
+# FCS_REFERENCE environment variable (the project root, holding src/ and
+# tutorial/), or from the record the last reference build left in _ref/.
+REF_ROOT_RECORD = os.path.join(HERE, "_ref", "REFERENCE_ROOT")
+
+
+def reference_root():
+    """The reference project's root directory, or None when it is unknown
+    or absent on this host."""
+    root = os.environ.get("FCS_REFERENCE")
+    if not root and os.path.exists(REF_ROOT_RECORD):
+        root = open(REF_ROOT_RECORD).read().strip()
+    return root if root and os.path.isdir(os.path.join(root, "src")) else None
+
+
+def reference_tutorial():
+    """The reference's tutorial tree (mechanisms and cases), or None."""
+    root = reference_root()
+    d = os.path.join(root, "tutorial") if root else None
+    return d if d and os.path.isdir(d) else None
 
 SOLVERS = {"OptRodas34": 0, "OptRosenbrock34": 1, "OptSeulex": 2, "OptRodas23": 3, "OptRosenbrock23": 4}
 
@@ -69,12 +91,57 @@ def _ptr(a, t=C.c_double):
     return None if a is None else a.ctypes.data_as(C.POINTER(t))
 
 
-def build(ref: bool = True):
-    """Compile the port (always) and the reference core (only when its sources
-    are present and the host is x86-64)."""
+def build(ref: bool = True, root: str | None = None):
+    """Compile the port (always) and the reference core where it can be built:
+
+    * x86-64 with the reference tree (``root``, else :func:`reference_root`):
+      from its sources with AVX2/FMA and libmvec, as the reference builds
+      itself; the sources it needs are also staged, unmodified, into
+      ``_ref/src`` (git-ignored) for hosts without the tree;
+    * other hosts (aarch64): from the staged copy, with ``simd_shim/`` for
+      ``<immintrin.h>`` and libmvec.
+
+    The root used is recorded in ``_ref/REFERENCE_ROOT``."""
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
-    if ref and os.path.isdir(REF_SRC) and os.uname().machine == "x86_64":
+    if not ref:
+        return
+    if root and not os.path.isdir(os.path.join(root, "src")):
+        root = None
+    root = root or reference_root()
+    if root:
+        src = os.path.join(root, "src")
+        subprocess.run(["make", "-s", "-C", HERE, "ref-stage", "REF=" + src], check=True)
+        with open(REF_ROOT_RECORD, "w") as f:
+            f.write(root + "\n")
+    if os.uname().machine == "x86_64":
+        if root:
+            subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + os.path.join(root, "src")], check=True)
+    elif os.path.exists(os.path.join(STAGED_SRC, "Reaction", "OptReaction.H")):
+        if os.path.exists(REF_SO) and not _native_elf(REF_SO):
+            os.remove(REF_SO)  # built on another architecture
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+def _native_elf(path) -> bool:
+    """Whether the shared object at `path` is for this host's architecture
+    (ELF e_machine: 62 x86-64, 183 aarch64)."""
+    want = {"x86_64": 62, "aarch64": 183}.get(os.uname().machine)
+    with open(path, "rb") as f:
+        head = f.read(20)
+    return len(head) == 20 and head[:4] == b"\x7fELF" and (want is None or int.from_bytes(head[18:20], "little") == want)
+
+
+def build_shim() -> str | None:
+    """The reference core built with the portable SIMD shim on this host (the
+    build the aarch64 hosts use), for checking the shim against the fixtures
+    made by the AVX2 build; None when the reference sources are absent."""
+    if os.uname().machine != "x86_64":
+        return REF_SO if os.path.exists(REF_SO) else None
+    root = reference_root()
+    if not root:
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, "ref-shim", "REF=" + os.path.join(root, "src")], check=True)
+    return REF_SHIM_SO
 
 
 class OrcOptions(C.Structure):
@@ -204,10 +271,10 @@ class Reference:
     """The reference core compiled from its own sources (x86-64 only)."""
 
     def __init__(self, flat, solver="OptRodas34", jacobian="exact", abs_tol=1e-8, rel_tol=1e-4,
-                 max_steps=10000):
-        if not os.path.exists(REF_SO):
+                 max_steps=10000, so=None):
+        if so is None and not os.path.exists(REF_SO):
             build(ref=True)
-        self.lib = C.CDLL(REF_SO)
+        self.lib = C.CDLL(so or REF_SO)
         L = self.lib
         L.ref_create.restype = C.c_void_p
         L.ref_create.argtypes = [C.POINTER(MechDesc), C.c_int, C.c_int, C.c_double, C.c_double, C.c_int]

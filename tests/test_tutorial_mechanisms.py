@@ -34,15 +34,15 @@ MECHS = [
 
 def _files(case):
     import oracle
-    d = os.path.join(oracle.REF_TUTORIAL, case, "constant")
+    d = os.path.join(oracle.reference_tutorial(), case, "constant")
     return os.path.join(d, "reactions"), os.path.join(d, "speciesThermo")
 
 
 @pytest.fixture(scope="module")
 def ref_available(port_built, lib_path):
     import oracle
-    if not os.path.isdir(oracle.REF_TUTORIAL):
-        pytest.skip("reference tutorials not present on this host")
+    if not oracle.reference_tutorial():
+        pytest.skip("reference tutorials not present on this host (set FCS_REFERENCE)")
     oracle.build(ref=True)
     if not os.path.exists(oracle.REF_SO):
         pytest.skip("reference core not built on this host")
