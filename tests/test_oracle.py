@@ -33,7 +33,8 @@ def _setup(case):
     return w, flat, solver, g, cells
 
 
-@pytest.mark.parametrize("case", CASES + ["ignition_10s_tight", "counterflow_53s_tight"])
+@pytest.mark.parametrize("case", CASES + ["ignition_10s_tight", "counterflow_53s_tight", "large_200s_tight",
+                                  "uneven_111s_OptRodas34", "large_200s_OptRodas34"])
 def test_generator_reproduces_fixture_inputs(case):
     fixture.check_generator(_golden(case), case.rsplit("_", 1)[0])
 
@@ -133,3 +134,31 @@ def test_port_tc_matches_reference_golden(wname, port_built):
     flat, cells = fixture.load_prefixed(g, wname + "__")
     tc = oracle.Port(flat).tc(cells.p, cells.T, cells.rho0, cells.Y)
     np.testing.assert_allclose(tc, g[wname + "__tc"], rtol=1e-13)
+
+
+@pytest.mark.parametrize("case", ["uneven_111s_OptRodas34", "large_200s_OptRodas34", "tutorial_nc12h26_narayanaswamy",
+                                  "tutorial_ic8h18_yoo", "tutorial_ch4_gri30_counterflow"])
+def test_port_matches_reference_on_large_and_tutorial_inputs(case, port_built):
+    """The 111- and 200-species fields and the reference's own tutorial
+    mechanisms (255 and 140 species) and counterflow-flame cells: the port
+    against the reference core's integration, RHS and Jacobian."""
+    import oracle
+    g = _golden(case)
+    flat, cells = fixture.load(g)
+    if case.startswith("tutorial"):
+        dt, treact = float(g["dt"]), 0.0
+    else:
+        w = fcs.WORKLOADS[case.rsplit("_", 1)[0]]
+        dt, treact = w.dt, w.treact
+    port = oracle.Port(flat)
+    out = port.integrate(cells, dt, abs_tol=float(g["abs_tol"]), rel_tol=float(g["rel_tol"]), treact=treact,
+                         threads=8)
+    assert (out["status"] == g["status"]).all()
+    np.testing.assert_allclose(out["T"], g["T"], rtol=1e-7, atol=0)
+    np.testing.assert_allclose(out["Y"], g["Y"], rtol=0, atol=1e-8)
+    assert abs(out["counters"]["jacobians"] - int(g["jacobians"])) <= max(4, 0.01 * int(g["jacobians"]))
+    f = port.rhs(cells.p, cells.T, cells.Y)
+    assert np.max(np.abs(f - g["rhs"]) / (np.abs(g["rhs"]).max(axis=1, keepdims=True) + 1e-300)) < 1e-12
+    k = g["jac"].shape[0]
+    J, _ = port.jacobian(cells.p[:k], cells.T[:k], cells.Y[:, :k])
+    assert np.max(np.abs(J - g["jac"]) / np.abs(g["jac"]).max(axis=(1, 2), keepdims=True)) < 1e-12
