@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--mapping", type=int, default=0)
     ap.add_argument("--cells", type=int, default=0, help="0: the workload's full cell count")
+    ap.add_argument("--dt", type=float, default=0.0,
+                    help="CFD step in s (0: the workload's); a shorter step makes a short launch for profiling")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--method", default="both", choices=["plain", "gated", "both", "mlp"],
@@ -83,6 +85,14 @@ def max_over_ranks(value: float, device=None) -> float:
     t = torch.tensor([value], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def workload(args):
+    """The named workload, with the CFD step replaced when --dt is given."""
+    import dataclasses
+    import fcs
+    w = fcs.WORKLOADS[args.workload]
+    return dataclasses.replace(w, dt=args.dt) if args.dt > 0 else w
 
 
 def dist_info():
@@ -353,7 +363,7 @@ def main():
     torch.cuda.set_device(local)
     import fcs
     from fcs import _lib, surrogate
-    w = fcs.WORKLOADS[args.workload]
+    w = workload(args)
     mech = w.mechanism()
     flat = fcs.flatten(mech)
     cells = fcs.cells_for(w, mech, n=args.cells or None)

@@ -8,8 +8,10 @@
 // by fcs_sync.
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cstring>
 #include <string>
+#include <thread>
 
 #include "../../include/fcs.h"
 #include "fcs_ctx.h"
@@ -27,16 +29,13 @@ extern "C" fcs_status fcs_integrate_async(fcs_ctx* ctx, int64_t nc, double dt, c
     if (!(dt > 0)) return set_err(ctx, FCS_ERR_INVALID, "delta_t must be positive");
     CK(cudaSetDevice(ctx->device));
     // the arrays must be device memory of this device: host memory would fault in the kernels
-    for (const void* a : {(const void*)p, (const void*)rho0, (const void*)T, (const void*)Y, (const void*)sub,
-                          (const void*)RR, (const void*)status}) {
-        if (!a) continue;
-        cudaPointerAttributes at{};
-        if (cudaPointerGetAttributes(&at, a) != cudaSuccess) {
-            cudaGetLastError();
-            return set_err(ctx, FCS_ERR_INVALID, "fcs_integrate_async takes device arrays only");
-        }
-        if (!((at.type == cudaMemoryTypeDevice && at.device == ctx->device) || at.type == cudaMemoryTypeManaged))
-            return set_err(ctx, FCS_ERR_INVALID, "fcs_integrate_async takes device arrays of the context's device");
+    {
+        const struct { const void* ptr; const char* name; size_t align; } arrays[] = {
+            {p, "p", 8}, {rho0, "rho0", 8}, {T, "T", 8}, {Y, "Y", 8}, {sub, "sub_delta_t", 8},
+            {RR, "RR", 8}, {status, "cell_status", 4}};
+        for (const auto& a : arrays)
+            if (a.ptr)
+                if (fcs_status s = check_device_array(ctx, a.ptr, a.name, a.align)) return s;
     }
     cudaStream_t st = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : ctx->stream;
     const int ns = ctx->M.ns;
@@ -84,10 +83,26 @@ extern "C" fcs_status fcs_integrate_async(fcs_ctx* ctx, int64_t nc, double dt, c
     return FCS_OK;
 }
 
-extern "C" fcs_status fcs_sync(fcs_ctx* ctx, fcs_step_stats* stats, double* dtMin) {
+static fcs_status sync_impl(fcs_ctx* ctx, double timeout_ms, fcs_step_stats* stats, double* dtMin) {
     if (!ctx) return FCS_ERR_INVALID;
     if (!ctx->asyncPending) return set_err(ctx, FCS_ERR_STATE, "no step in flight");
     CK(cudaSetDevice(ctx->device));
+    if (timeout_ms >= 0) {
+        // bounded host-side wait: poll the step's event until it completes or
+        // the limit runs out; the step itself is left running and stays
+        // pending, so a later fcs_sync / fcs_sync_timeout collects it
+        const auto t0 = std::chrono::steady_clock::now();
+        for (;;) {
+            const cudaError_t q = cudaEventQuery(ctx->evAsync);
+            if (q == cudaSuccess) break;
+            if (q != cudaErrorNotReady) return cuda_err(ctx, q, "cudaEventQuery(step)");
+            const double el =
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            if (el >= timeout_ms)
+                return set_err(ctx, FCS_ERR_TIMEOUT, "the step did not complete within the wait limit");
+            std::this_thread::sleep_for(std::chrono::microseconds(el < 1.0 ? 20 : 200));
+        }
+    }
     ctx->asyncPending = false;
     CK(cudaEventSynchronize(ctx->evAsync));
     const long long* hs = ctx->hStats;
@@ -118,4 +133,13 @@ extern "C" fcs_status fcs_sync(fcs_ctx* ctx, fcs_step_stats* stats, double* dtMi
     }
     if (hs[ST_FAILED] > 0) return set_err(ctx, FCS_ERR_CELLS, "some cells failed; see cell_status");
     return FCS_OK;
+}
+
+extern "C" fcs_status fcs_sync(fcs_ctx* ctx, fcs_step_stats* stats, double* dtMin) {
+    return sync_impl(ctx, -1.0, stats, dtMin);
+}
+
+extern "C" fcs_status fcs_sync_timeout(fcs_ctx* ctx, double timeout_ms, fcs_step_stats* stats, double* dtMin) {
+    if (!(timeout_ms >= 0)) return set_err(ctx, FCS_ERR_INVALID, "timeout_ms must be >= 0");
+    return sync_impl(ctx, timeout_ms, stats, dtMin);
 }

@@ -4,9 +4,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <cstdint>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -16,6 +19,7 @@
 #include "../../include/fcs.h"
 #include "fcs_device.cuh"
 #include "fcs_internal.h"
+#include "fcs_lane_layout.h"
 #include "fcs_launch.h"
 #include "fcs_ctx.h"
 
@@ -28,7 +32,51 @@ fcs_status fcs::set_err(fcs_ctx* c, fcs_status s, const std::string& m) {
 }
 
 fcs_status fcs::cuda_err(fcs_ctx* c, cudaError_t e, const char* where) {
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();  // not sticky: the context stays usable
+        return set_err(c, FCS_ERR_NOMEM, std::string(where) + ": " + cudaGetErrorString(e));
+    }
     return set_err(c, FCS_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+fcs_status fcs::refuse_if_async_pending(fcs_ctx* ctx) {
+    if (ctx && ctx->asyncPending)
+        return set_err(ctx, FCS_ERR_STATE, "a step from fcs_integrate_async is in flight: call fcs_sync first");
+    return FCS_OK;
+}
+
+fcs_status fcs::check_device_array(fcs_ctx* ctx, const void* ptr, const char* name, size_t align) {
+    if (reinterpret_cast<uintptr_t>(ptr) % align != 0)
+        return set_err(ctx, FCS_ERR_INVALID, std::string(name) + " is not aligned");
+    cudaPointerAttributes a{};
+    const cudaError_t e = cudaPointerGetAttributes(&a, ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(ctx, FCS_ERR_INVALID, std::string(name) + " is not a device pointer");
+    }
+    const bool ok = (a.type == cudaMemoryTypeDevice && a.device == ctx->device) || a.type == cudaMemoryTypeManaged;
+    if (!ok)
+        return set_err(ctx, FCS_ERR_INVALID,
+                       std::string(name) + " must be device memory of the context's device (without "
+                                           "FCS_PTR_DEVICE the entry points take host arrays)");
+    return FCS_OK;
+}
+
+namespace {
+std::atomic<int> g_injected_alloc_failures{0};
+}
+
+bool fcs::take_injected_alloc_failure() {
+    int k = g_injected_alloc_failures.load();
+    while (k > 0)
+        if (g_injected_alloc_failures.compare_exchange_weak(k, k - 1)) return true;
+    return false;
+}
+
+extern "C" fcs_status fcs_test_fail_allocations(int32_t count) {
+    if (count < 0) return FCS_ERR_INVALID;
+    g_injected_alloc_failures.store(count);
+    return FCS_OK;
 }
 
 
@@ -75,6 +123,8 @@ extern "C" fcs_status fcs_create(fcs_ctx** out, int device) {
 extern "C" fcs_status fcs_destroy(fcs_ctx* ctx) {
     if (!ctx) return FCS_OK;
     cudaSetDevice(ctx->device);
+    // a step from fcs_integrate_async may still run on the caller's stream
+    if (ctx->asyncPending && ctx->evAsync) cudaEventSynchronize(ctx->evAsync);
     cudaStreamSynchronize(ctx->stream);
     gate_release(ctx);
     for (DBuf<double>* b : {&ctx->dW, &ctx->dInvW, &ctx->dTc, &ctx->dCoef, &ctx->dEff, &ctx->dPlogRow,
@@ -109,8 +159,8 @@ extern "C" fcs_status fcs_set_options(fcs_ctx* ctx, const fcs_options* o) {
     if (!(o->abs_tol > 0) || !(o->rel_tol > 0)) return set_err(ctx, FCS_ERR_INVALID, "tolerances must be positive");
     if (o->max_steps <= 0 || o->max_rejects <= 0) return set_err(ctx, FCS_ERR_INVALID, "maxSteps must be positive");
     const int m = o->mapping;
-    if (m != 0 && m != 32 && m != 64 && m != 128 && m != 256)
-        return set_err(ctx, FCS_ERR_INVALID, "mapping must be auto, 32, 64, 128 or 256");
+    if (m != 0 && m != 1 && m != 32 && m != 64 && m != 128 && m != 256)
+        return set_err(ctx, FCS_ERR_INVALID, "mapping must be auto, lane (1), 32, 64, 128 or 256");
     ctx->opt = *o;
     return FCS_OK;
 }
@@ -128,6 +178,7 @@ extern "C" fcs_status fcs_mechanism_size(const fcs_ctx* ctx, int32_t* ns, int32_
 
 extern "C" fcs_status fcs_load_mechanism(fcs_ctx* ctx, const fcs_mechanism_desc* d) {
     if (!ctx || !d) return FCS_ERR_INVALID;
+    if (fcs_status s = refuse_if_async_pending(ctx)) return s;
     const int ns = d->n_species, nr = d->n_reactions;
     if (ns < 1 || nr < 0) return set_err(ctx, FCS_ERR_INVALID, "bad species/reaction count");
     if (ns > 255) return set_err(ctx, FCS_ERR_UNSUPPORTED, "the GPU path handles up to 255 species");
@@ -327,8 +378,38 @@ KOpts fcs::kopts(const fcs_options& o) {
     return k;
 }
 
+// Lane per cell (FCS_MAPPING_LANE): blocks of 128 threads, as many per SM
+// as the registers allow (at most 4), a global-memory workspace of
+// make_lane_layout(...).words doubles per thread.  Rosenbrock-family solvers
+// in FP64 only.
+static bool make_lane_shape(fcs_ctx* ctx, bool integrate, Shape& sh) {
+    const fcs_options& o = ctx->opt;
+    const bool mixed = o.precision == FCS_PRECISION_MIXED;
+    if (!integrate || o.solver == FCS_SOLVER_SEULEX || mixed) return false;
+    int maxThreads = 0, regs = 0;
+    if (integrate_attributes(1, mixed, &maxThreads, &regs) != cudaSuccess) return false;
+    constexpr int kBlock = 128;
+    if (maxThreads < kBlock) return false;
+    int perSM = std::max(1, std::min(4, 65536 / std::max(1, regs * kBlock)));
+    // FCS_LANE_BLOCKS_PER_SM caps the resident blocks (fewer lanes than cells
+    // lets lanes take several cells each and balance uneven cells)
+    if (const char* e = std::getenv("FCS_LANE_BLOCKS_PER_SM")) {
+        const int v = std::atoi(e);
+        if (v >= 1) perSM = std::min(perSM, v);
+    }
+    sh.mixed = mixed;
+    sh.global = true;
+    sh.lc.group = 1;
+    sh.lc.block = kBlock;
+    sh.lc.grid = ctx->numSMs * perSM;
+    sh.L = SlotLayout{};
+    sh.L.bytes = make_lane_layout(ctx->M.ns, ctx->M.nTB, mixed).words * (int)sizeof(double);
+    return true;
+}
+
 // Build the launch shape for a group size; returns false when impossible.
 bool fcs::make_shape(fcs_ctx* ctx, int group, bool integrate, Shape& sh) {
+    if (group == FCS_MAPPING_LANE) return make_lane_shape(ctx, integrate, sh);
     const fcs_options& o = ctx->opt;
     const bool mixed = o.precision == FCS_PRECISION_MIXED;
     const bool seulex = integrate && o.solver == FCS_SOLVER_SEULEX;
@@ -461,12 +542,21 @@ static fcs_status integrate_impl(fcs_ctx* ctx, int64_t nc, double dt, const doub
                                  double* dtMin, int32_t flags) {
     if (!ctx) return FCS_ERR_INVALID;
     if (!ctx->loaded) return set_err(ctx, FCS_ERR_STATE, "no mechanism loaded");
+    if (fcs_status s = refuse_if_async_pending(ctx)) return s;
     if (nc < 0 || nc > (int64_t)INT32_MAX) return set_err(ctx, FCS_ERR_INVALID, "n_cells out of range");
     if (!p || !rho0 || !T || !Y || !sub) return set_err(ctx, FCS_ERR_INVALID, "null cell array");
     if (!dtc && !(dt > 0)) return set_err(ctx, FCS_ERR_INVALID, "delta_t must be positive");
     cudaSetDevice(ctx->device);
     const int ns = ctx->M.ns;
     const bool dev = flags & FCS_PTR_DEVICE;
+    if (dev) {
+        const struct { const void* ptr; const char* name; size_t align; } arrays[] = {
+            {p, "p", 8}, {rho0, "rho0", 8}, {T, "T", 8}, {Y, "Y", 8}, {sub, "sub_delta_t", 8},
+            {RR, "RR", 8}, {status, "cell_status", 4}, {dtc, "delta_t", 8}};
+        for (const auto& a : arrays)
+            if (a.ptr)
+                if (fcs_status s = check_device_array(ctx, a.ptr, a.name, a.align)) return s;
+    }
     cudaStream_t st = ctx->stream;
     CellIO io{};
     io.nCells = nc;
@@ -649,6 +739,7 @@ static fcs_status eval_impl(fcs_ctx* ctx, int64_t nc, const double* p, const dou
                             const double* Y, double* out, double* J, double* Qdot, int mode, int32_t flags) {
     if (!ctx) return FCS_ERR_INVALID;
     if (!ctx->loaded) return set_err(ctx, FCS_ERR_STATE, "no mechanism loaded");
+    if (fcs_status s = refuse_if_async_pending(ctx)) return s;
     if (nc < 0 || nc > (int64_t)INT32_MAX) return set_err(ctx, FCS_ERR_INVALID, "n_cells out of range");
     if (!p || !T || !Y || !out) return set_err(ctx, FCS_ERR_INVALID, "null array");
     if (nc == 0) return FCS_OK;
@@ -675,7 +766,8 @@ static fcs_status eval_impl(fcs_ctx* ctx, int64_t nc, const double* p, const dou
         if (J) { CK(ctx->bJ.ensure((size_t)n * n * nc)); dJ = ctx->bJ.p; }
         if (Qdot) { CK(ctx->bQ.ensure(nc)); dQ = ctx->bQ.p; }
     }
-    const int group = ctx->opt.mapping ? ctx->opt.mapping : default_group(ctx);
+    // the per-cell evaluations run on cell groups (the lane mapping is the integrator's)
+    const int group = ctx->opt.mapping > FCS_MAPPING_LANE ? ctx->opt.mapping : default_group(ctx);
     Shape sh;
     if (!make_shape(ctx, group, false, sh)) return set_err(ctx, FCS_ERR_UNSUPPORTED, "no launch shape");
     const int gpb = sh.lc.block / sh.lc.group;

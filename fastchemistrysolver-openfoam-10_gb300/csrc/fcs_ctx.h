@@ -16,6 +16,11 @@
 
 namespace fcs {
 
+// Allocation failures injected by fcs_test_fail_allocations (host side: the
+// next k growths of a device buffer report cudaErrorMemoryAllocation without
+// calling cudaMalloc).
+bool take_injected_alloc_failure();
+
 template<class T>
 struct DBuf {
     T* p = nullptr;
@@ -25,6 +30,7 @@ struct DBuf {
         if (p) cudaFree(p);
         p = nullptr;
         n = 0;
+        if (take_injected_alloc_failure()) return cudaErrorMemoryAllocation;
         cudaError_t e = cudaMalloc(&p, std::max<size_t>(want, 1) * sizeof(T));
         if (e == cudaSuccess) n = want;
         return e;
@@ -98,7 +104,16 @@ struct fcs_ctx {
 namespace fcs {
 
 fcs_status set_err(fcs_ctx* c, fcs_status s, const std::string& m);
+// FCS_ERR_NOMEM for a failed allocation, FCS_ERR_CUDA otherwise
 fcs_status cuda_err(fcs_ctx* c, cudaError_t e, const char* where);
+// FCS_ERR_STATE while an fcs_integrate_async step is in flight on this
+// context: its kernels read the context's queue, counters, workspace and
+// mechanism, and fcs_sync reads its events and pinned statistics.
+fcs_status refuse_if_async_pending(fcs_ctx* ctx);
+// A cell array handed over as device memory must be device (or managed)
+// memory of the context's device, aligned to `align` bytes: host memory
+// handed to a kernel would fault.
+fcs_status check_device_array(fcs_ctx* ctx, const void* ptr, const char* name, size_t align);
 KOpts kopts(const fcs_options& o);
 // Launch shape for a group size; false when impossible.
 bool make_shape(fcs_ctx* ctx, int group, bool integrate, Shape& sh);

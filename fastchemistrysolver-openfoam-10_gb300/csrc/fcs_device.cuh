@@ -574,15 +574,15 @@ static __device__ __noinline__ FalloffK falloff_rate(const DevMech& M, const Rxn
 // and dKf/dM, dKr/dM (Jacobian.C:401-422).
 struct SpecialK { double Kf, dKfdT, dKfdC, Kr, dKrdT, dKrdC; };
 
-static __device__ __forceinline__ SpecialK special_rates(const DevMech& M, const RxnInfo& x, const double* Mtb,
-                                                      double Tc, double logT, double invT, bool deriv) {
+// Mt: the reaction's third-body concentration (1 when it has none).
+static __device__ __forceinline__ SpecialK special_rates_m(const DevMech& M, const RxnInfo& x, const double Mt,
+                                                        double Tc, double logT, double invT, bool deriv) {
     SpecialK o{0, 0, 0, 0, 0, 0};
     double K0 = x.A, dK0dT = 0;
     if (!x.tind) {
         K0 = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
         dK0dT = K0 * (fma(x.Ta, invT, x.beta) * invT);
     }
-    const double Mt = x.tb >= 0 ? Mtb[x.tb] : 1.0;
     if (x.fo >= 0) {
         const FalloffK k = falloff_rate(M, x, K0, dK0dT, Mt, Tc, logT, invT, deriv);
         o.Kf = k.Kf;
@@ -611,6 +611,11 @@ static __device__ __forceinline__ SpecialK special_rates(const DevMech& M, const
         }
     }
     return o;
+}
+
+static __device__ __forceinline__ SpecialK special_rates(const DevMech& M, const RxnInfo& x, const double* Mtb,
+                                                      double Tc, double logT, double invT, bool deriv) {
+    return special_rates_m(M, x, x.tb >= 0 ? Mtb[x.tb] : 1.0, Tc, logT, invT, deriv);
 }
 
 // ------------------------------------------------------------------------

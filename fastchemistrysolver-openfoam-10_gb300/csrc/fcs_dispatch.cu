@@ -91,6 +91,7 @@ cudaError_t launch_integrate(const LaunchCfg& lc, bool mixed, const DevMech& M, 
                              const SlotLayout& L, const CellIO& io, const WorkQueue& q, char* gws,
                              cudaStream_t st) {
     switch (lc.group) {
+        case 1: return launch_lane_integrate(lc, mixed, M, o, io, q, gws, st);
         case 32: return launch_integrate_g<32>(lc, mixed, M, o, L, io, q, gws, st);
         case 64: return launch_integrate_g<64>(lc, mixed, M, o, L, io, q, gws, st);
         case 128: return launch_integrate_g<128>(lc, mixed, M, o, L, io, q, gws, st);
@@ -114,6 +115,7 @@ cudaError_t launch_eval(const LaunchCfg& lc, bool mixed, const DevMech& M, const
 
 cudaError_t integrate_attributes(int group, bool mixed, int* maxThreads, int* regs) {
     switch (group) {
+        case 1: return lane_attributes(mixed, maxThreads, regs);
         case 32: return integrate_attributes_g<32>(mixed, maxThreads, regs);
         case 64: return integrate_attributes_g<64>(mixed, maxThreads, regs);
         case 128: return integrate_attributes_g<128>(mixed, maxThreads, regs);

@@ -251,10 +251,12 @@ extern "C" fcs_status fcs_surrogate_attach(fcs_ctx* ctx, fcs_mlp* mlp, int32_t n
                                            const double* emass, const fcs_gate_options* opts) {
     if (!ctx) return FCS_ERR_INVALID;
     if (!mlp) {
+        if (fcs_status s = refuse_if_async_pending(ctx)) return s;
         gate_release(ctx);
         return FCS_OK;
     }
     if (!ctx->loaded) return set_err(ctx, FCS_ERR_STATE, "no mechanism loaded");
+    if (fcs_status s = refuse_if_async_pending(ctx)) return s;
     const int ns = ctx->M.ns;
     if (mlp_n_in(mlp) != ns + 3 || mlp_n_out(mlp) != ns + 2)
         return set_err(ctx, FCS_ERR_INVALID, "surrogate must have Ns+3 inputs and Ns+2 outputs");
@@ -292,12 +294,21 @@ extern "C" fcs_status fcs_integrate_gated(fcs_ctx* ctx, int64_t nc, double dt, c
     if (!ctx->loaded) return set_err(ctx, FCS_ERR_STATE, "no mechanism loaded");
     GateState* g = ctx->gate;
     if (!g) return set_err(ctx, FCS_ERR_STATE, "no surrogate attached");
+    if (fcs_status s = refuse_if_async_pending(ctx)) return s;
     if (nc < 0 || nc > (int64_t)INT32_MAX) return set_err(ctx, FCS_ERR_INVALID, "n_cells out of range");
     if (!p || !rho0 || !T || !Y || !sub) return set_err(ctx, FCS_ERR_INVALID, "null cell array");
     if (!(dt > 0)) return set_err(ctx, FCS_ERR_INVALID, "delta_t must be positive");
     cudaSetDevice(ctx->device);
     const int ns = ctx->M.ns;
     const bool dev = flags & FCS_PTR_DEVICE;
+    if (dev) {
+        const struct { const void* ptr; const char* name; size_t align; } arrays[] = {
+            {p, "p", 8}, {rho0, "rho0", 8}, {T, "T", 8}, {Y, "Y", 8}, {sub, "sub_delta_t", 8},
+            {RR, "RR", 8}, {status, "cell_status", 4}};
+        for (const auto& a : arrays)
+            if (a.ptr)
+                if (fcs_status s = check_device_array(ctx, a.ptr, a.name, a.align)) return s;
+    }
     cudaStream_t st = ctx->stream;
     const int E = mlp_members(g->mlp), nIn = ns + 3, nOut = ns + 2;
     CellIO io{};

@@ -1,0 +1,995 @@
+#pragma once
+// fcs_lane.cuh -- the lane-per-cell mapping of the Rosenbrock-family
+// integrator (OptRodas34, OptRosenbrock34, OptRodas23, OptRosenbrock23).
+//
+// One thread integrates one cell from start to end of the CFD step.  The 32
+// lanes of a warp therefore run the same instruction stream on 32 different
+// cells: every FP64 instruction carries 32 useful lanes, no barrier or
+// cross-lane reduction is needed, and the mechanism data each instruction
+// reads (one reaction record, one species' coefficients) is the same address
+// for the whole warp (a broadcast from L1).  The cells' working sets live in
+// a global-memory workspace interleaved across the lanes (fcs_lane_layout.h),
+// so each per-lane array access of a warp is one 256-byte transaction.
+//
+// The attempt (Jacobian, LU, stages, error norm) is identical code for every
+// cell; only the step-size controller and the cell hand-over differ between
+// lanes.  A lane whose cell is done takes the next cell from the device work
+// queue on its own (warp-aggregated atomic), so the lanes of a warp stay busy
+// until the queue runs dry.
+//
+// Arithmetic follows the cell-group kernels (fcs_kernels.cuh) operation by
+// operation -- the same rate expressions, the same order of every species and
+// Jacobian accumulation (reaction order), the same LU with the reference's
+// panel-local pivoting (the delayed 4-column update below applies each
+// element's multiply-adds in the same order as the column-by-column
+// version), the same solves -- except that the sums over species of the
+// mixture scalars (rho M, Cp M, ...) run serially here instead of as
+// butterfly reductions.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "fcs_device.cuh"
+#include "fcs_kernels.cuh"
+#include "fcs_lane_layout.h"
+#include "fcs_launch.h"
+
+namespace fcs {
+
+constexpr int kLanes = 32;
+
+// A per-lane array: element e of this lane's array at p[e * 32].
+template<class T>
+struct LA {
+    T* p;
+    __device__ __forceinline__ T& operator[](int e) const { return p[(size_t)e * kLanes]; }
+    __device__ __forceinline__ LA operator+(int e) const { return LA{p + (size_t)e * kLanes}; }
+};
+
+struct LaneSlot {
+    int n, ns;
+    LA<double> A, vec, C, B, Binv, Cp, Ha, dBdT, Mtb, tbF, invD;
+    LA<int> piv;
+    LA<float> LU32, x32;   // mixed precision
+    LA<double> dr, dc;     // mixed precision equilibration
+    __device__ __forceinline__ LA<double> v(int k) const { return vec + k * n; }
+};
+
+__device__ __forceinline__ LaneSlot make_lane_slot(double* ws, const LaneLayout& L) {
+    // ws: this warp's workspace; lane offset applied here
+    const int lane = threadIdx.x & 31;
+    double* base = ws + lane;
+    LaneSlot s;
+    s.n = L.n;
+    s.ns = L.ns;
+    s.A = LA<double>{base + (size_t)L.offA * kLanes};
+    s.vec = LA<double>{base + (size_t)L.offVec * kLanes};
+    const LA<double> sp{base + (size_t)L.offSp * kLanes};
+    s.C = sp; s.B = sp + L.ns; s.Binv = sp + 2 * L.ns; s.Cp = sp + 3 * L.ns; s.Ha = sp + 4 * L.ns;
+    s.dBdT = sp + 5 * L.ns;
+    const int nt = L.nTB > 0 ? L.nTB : 1;
+    s.Mtb = LA<double>{base + (size_t)L.offTb * kLanes};
+    s.tbF = s.Mtb + nt;
+    s.invD = LA<double>{base + (size_t)L.offInvD * kLanes};
+    s.piv = LA<int>{reinterpret_cast<int*>(ws + (size_t)L.offPiv * kLanes) + lane};
+    s.LU32 = LA<float>{reinterpret_cast<float*>(ws + (size_t)L.offLU32 * kLanes) + lane};
+    s.dr = LA<double>{base + (size_t)L.offScale * kLanes};
+    s.dc = s.dr + L.n;
+    s.x32 = LA<float>{reinterpret_cast<float*>(ws + (size_t)L.offX32 * kLanes) + lane};
+    return s;
+}
+
+// ------------------------------------------------------------------------
+// rates
+
+// 1/Kc with the reference's clamp (inv_equilibrium_kc over per-lane arrays)
+__device__ __forceinline__ double lane_inv_kc(const RxnInfo& x, const LA<double>& E, const LA<double>& Einv,
+                                              const PFactor& pf) {
+    double v = E[x.sl[0]];
+    #pragma unroll 1
+    for (int q = 1; q < x.nl; q++) v *= E[x.sl[q]];
+    #pragma unroll 1
+    for (int q = 0; q < x.nr; q++) v *= Einv[x.sr[q]];
+    if (x.dnu != 0) v *= pressure_factor(pf, x.dnu);
+    const double cl = inv_kc_clamp(x);
+    return v > cl ? cl : v;
+}
+
+// Third-body concentrations M_t = sum_j eff[t][j] C_j (ThirdBodyFactor1D)
+__device__ __forceinline__ void lane_third_body(const DevMech& M, const LaneSlot& s) {
+    const int ns = M.ns;
+    #pragma unroll 1
+    for (int t = 0; t < M.nTB; t++) {
+        const double* e = M.eff + (size_t)t * ns;
+        double m = 0;
+        #pragma unroll 4
+        for (int j = 0; j < ns; j++) m = fma(__ldg(&e[j]), s.C[j], m);
+        s.Mtb[t] = m;
+    }
+}
+
+// Forward rate constant of an ordinary (not special-block) reaction; PLOG
+// also returns dk/dT.
+__device__ __forceinline__ double lane_kf(const DevMech& M, const RxnInfo& x, double p, double logP, double logT,
+                                          double invT, double* dkdT) {
+    double Kf;
+    if (x.kind == FCS_RXN_PLOG) {
+        Kf = plog_rate(M, x.plog, p, logP, logT, invT, dkdT);
+    } else if (x.tind) {
+        Kf = x.A;
+        *dkdT = 0;
+    } else {
+        Kf = x.A * fast_exp(fma(x.beta, logT, -(x.Ta * invT)));
+        *dkdT = Kf * (fma(x.Ta, invT, x.beta) * invT);
+    }
+    return Kf;
+}
+
+// RHS: FastChemistryModel::derivatives (FastChemistryModel.C:194-273 for mode
+// 1, 340-417 for mode 2) over OptReaction::dNdtByV (ReactionRate.C:732-1503).
+// YT is clamped (Y >= 0) in place; out[0..n) receives dY/dt and dT/dt.
+__device__ __noinline__ void lane_rhs(const DevMech& M, const LaneSlot& s, double p, LA<double> YT,
+                                      LA<double> out, int mode) {
+    const int ns = M.ns;
+    const double T = YT[ns];
+    const double Tc = clampT(M, T);
+    const double RuTByP = kRu * T / p;
+    double part = 0;
+    #pragma unroll 1
+    for (int i = 0; i < ns; i++) {
+        const double y0 = YT[i];
+        const double y = y0 > 0 ? y0 : 0.0;
+        YT[i] = y;
+        part = fma(y * __ldg(&M.invW[i]), RuTByP, part);
+    }
+    const double invrhoM = part;
+    const double rhoM = 1.0 / invrhoM;
+    const double logT = log(Tc), invT = 1.0 / Tc;
+    const double Tp = mode == 2 ? T : Tc;
+    #pragma unroll 1
+    for (int i = 0; i < ns; i++) {
+        const double invW = __ldg(&M.invW[i]);
+        s.C[i] = rhoM * invW * YT[i];
+        const Nasa a = load_nasa(species_coeffs(M, i, Tc));
+        const double Ei = fast_exp(gibbs_exponent(a, Tc, invT, logT));
+        s.B[i] = Ei;
+        s.Binv[i] = 1.0 / Ei;
+        const double RuInvW = invW * kRu;
+        s.Cp[i] = cp_of(a, Tp, RuInvW);
+        s.Ha[i] = ha_of(a, Tp, RuInvW);
+        out[i] = 0.0;
+    }
+    lane_third_body(M, s);
+    const PFactor pf = pressure_factors(Tc);
+    const double logP = M.nPlog ? log(p) : 0.0;
+    const int sp0 = M.spBegin, sp1 = M.spBegin + M.nSp;
+    #pragma unroll 1
+    for (int r = 0; r < M.nr; r++) {
+        const RxnInfo x = load_rx(M.rx + r);
+        double Kf, Kr = 0;
+        if (r >= sp0 && r < sp1) {
+            const SpecialK k = special_rates_m(M, x, x.tb >= 0 ? s.Mtb[x.tb] : 1.0, Tc, logT, invT, false);
+            Kf = k.Kf;
+            Kr = k.Kr;  // non-equilibrium: its own reverse rate
+            if (x.rev == 1) Kr = Kf * lane_inv_kc(x, s.B, s.Binv, pf);
+        } else {
+            double dk;
+            Kf = lane_kf(M, x, p, logP, logT, invT, &dk);
+            if (x.tb >= 0) Kf *= s.Mtb[x.tb];
+            if (x.rev) Kr = Kf * lane_inv_kc(x, s.B, s.Binv, pf);
+        }
+        double CF = s.C[x.sl[0]];
+        #pragma unroll 1
+        for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
+        double CR = s.C[x.sr[0]];
+        #pragma unroll 1
+        for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
+        const double qr = Kf * CF - Kr * CR;
+        #pragma unroll 1
+        for (int q = 0; q < x.nl; q++) { double& w = out[x.sl[q]]; w = w - qr; }
+        #pragma unroll 1
+        for (int q = 0; q < x.nr; q++) { double& w = out[x.sr[q]]; w = w + qr; }
+    }
+    double cpm = 0, dtd = 0;
+    #pragma unroll 1
+    for (int i = 0; i < ns; i++) {
+        const double dY = (__ldg(&M.W[i]) * invrhoM) * out[i];
+        out[i] = dY;
+        cpm = fma(YT[i], s.Cp[i], cpm);
+        dtd = fma(s.Ha[i], dY, dtd);
+    }
+    out[ns] = -dtd / cpm;
+}
+
+// Analytic Jacobian (FastChemistryModel::jacobian, FastChemistryModel.C:489-572,
+// over ddNdtByVdcTp, Jacobian.C:5-1004, and the dC/dY conversion,
+// Jacobian.C:2814-2858 exact / 4541-4568 fast, 3709-3793 T column and row)
+// into J (row-major n x n), f = dy/dt; YT clamped in place.  tcAcc: a free
+// n-vector for the temperature-column sums.
+__device__ __noinline__ void lane_jac(const DevMech& M, const LaneSlot& s, double p, LA<double> YT, LA<double> f,
+                                      LA<double> J, LA<double> tcAcc, int fast) {
+    const int ns = M.ns, n = M.n;
+    #pragma unroll 1
+    for (int i = 0; i < ns; i++) {
+        const double y0 = YT[i];
+        YT[i] = y0 > 0 ? y0 : 0.0;
+    }
+    const double T = YT[ns];
+    const double Tc = clampT(M, T);
+    const double RuTByP = (kRu * Tc) / p;
+    double rs = 0, mws = 0;
+    #pragma unroll 1
+    for (int i = 0; i < ns; i++) {
+        const double y = YT[i], invW = __ldg(&M.invW[i]);
+        rs = fma(RuTByP, y * invW, rs);
+        mws = fma(y, invW, mws);
+    }
+    const double logT = log(Tc), invT = 1.0 / Tc;
+    const double rhoM = 1.0 / rs, invRhoM = rs, MW = 1.0 / mws;
+    double cpm = 0, dcpm = 0;
+    #pragma unroll 1
+    for (int i = 0; i < ns; i++) {
+        const double y = YT[i], invW = __ldg(&M.invW[i]);
+        const Nasa a = load_nasa(species_coeffs(M, i, Tc));
+        s.C[i] = rhoM * y * invW;
+        const double Ei = fast_exp(gibbs_exponent(a, Tc, invT, logT));
+        s.B[i] = Ei;
+        s.Binv[i] = 1.0 / Ei;
+        s.dBdT[i] = fma(fma(a.a5, invT, a.a0), invT,
+                        fma(fma(fma(a.a4 * 0.2, Tc, a.a3 * 0.25), Tc, a.a2 * (1.0 / 3.0)), Tc, a.a1 * 0.5));
+        const double RuInvW = invW * kRu;
+        const double cp = cp_of(a, Tc, RuInvW);
+        const double dcp = RuInvW * fma(Tc, fma(Tc, fma(Tc, 4 * a.a4, 3 * a.a3), 2 * a.a2), a.a1);
+        s.Cp[i] = cp;
+        s.Ha[i] = ha_of(a, Tc, RuInvW);
+        cpm = fma(y, cp, cpm);
+        dcpm = fma(y, dcp, dcpm);
+        f[i] = 0.0;
+        tcAcc[i] = 0.0;
+    }
+    const double CpM = cpm, dCpMdT = dcpm;
+    lane_third_body(M, s);
+    #pragma unroll 1
+    for (int idx = 0; idx < ns * n; idx++) J[idx] = 0.0;
+    const PFactor pf = pressure_factors(Tc);
+    const double logP = M.nPlog ? log(p) : 0.0;
+    const int sp0 = M.spBegin, sp1 = M.spBegin + M.nSp;
+    #pragma unroll 1
+    for (int r = 0; r < M.nr; r++) {
+        const RxnInfo x = load_rx(M.rx + r);
+        double Kf, dKfdT, dKfdC = 0, Kr = 0, dKrdT = 0, dKrdC = 0;
+        bool viaKc = false;
+        if (r >= sp0 && r < sp1) {
+            const SpecialK k = special_rates_m(M, x, x.tb >= 0 ? s.Mtb[x.tb] : 1.0, Tc, logT, invT, true);
+            Kf = k.Kf; dKfdT = k.dKfdT; dKfdC = k.dKfdC;
+            Kr = k.Kr; dKrdT = k.dKrdT; dKrdC = k.dKrdC;
+            viaKc = x.rev == 1;
+        } else {
+            Kf = lane_kf(M, x, p, logP, logT, invT, &dKfdT);
+            if (x.tb >= 0) {
+                const double Mt = s.Mtb[x.tb];
+                dKfdC = Kf;
+                Kf *= Mt;
+                dKfdT *= Mt;
+            }
+            viaKc = x.rev != 0;
+        }
+        if (viaKc) {
+            // Kr, dKr/dT and dKr/dM through Kc (JF* reversible branch); the Kc
+            // term of dKr/dT is dropped when Kc sits on its clamp
+            // (JacobianFunctionI.H:246-249)
+            const double invKc = lane_inv_kc(x, s.B, s.Binv, pf);
+            double sv = s.dBdT[x.sr[0]];
+            #pragma unroll 1
+            for (int q = 1; q < x.nr; q++) sv += s.dBdT[x.sr[q]];
+            double sl = s.dBdT[x.sl[0]];
+            #pragma unroll 1
+            for (int q = 1; q < x.nl; q++) sl += s.dBdT[x.sl[q]];
+            const double dKcdTByKc = (sv - sl) - x.dnu * invT;
+            Kr = Kf * invKc;
+            dKrdT = dKfdT * invKc - (invKc < inv_kc_clamp(x) ? Kr * dKcdTByKc : 0.0);
+            dKrdC = dKfdC * invKc;
+        }
+        double CF = s.C[x.sl[0]];
+        #pragma unroll 1
+        for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
+        double CR = s.C[x.sr[0]];
+        #pragma unroll 1
+        for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
+        const double qr = Kf * CF - Kr * CR;
+        const double dq = dKfdT * CF - dKrdT * CR;
+        if (x.tb >= 0) s.tbF[x.tb] = dKfdC * CF - dKrdC * CR;
+        #pragma unroll 1
+        for (int q = 0; q < x.nl; q++) {
+            const int i = x.sl[q];
+            f[i] = f[i] - qr;
+            tcAcc[i] = tcAcc[i] - dq;
+        }
+        #pragma unroll 1
+        for (int q = 0; q < x.nr; q++) {
+            const int i = x.sr[q];
+            f[i] = f[i] + qr;
+            tcAcc[i] = tcAcc[i] + dq;
+        }
+        // d q / d C_j for each reactant occurrence j: Kf times the other
+        // reactant concentrations (the first occurrence of j skipped),
+        // scattered down column j to the rows of the reaction
+        #pragma unroll 1
+        for (int qa = 0; qa < x.nl; qa++) {
+            const int j = x.sl[qa];
+            double d = Kf;
+            bool skipped = false;
+            #pragma unroll 1
+            for (int q = 0; q < x.nl; q++) {
+                if (!skipped && x.sl[q] == j) { skipped = true; continue; }
+                d *= s.C[x.sl[q]];
+            }
+            #pragma unroll 1
+            for (int q = 0; q < x.nl; q++) { double& c = J[x.sl[q] * n + j]; c = c - d; }
+            #pragma unroll 1
+            for (int q = 0; q < x.nr; q++) { double& c = J[x.sr[q] * n + j]; c = c + d; }
+        }
+        if (x.rev) {
+            #pragma unroll 1
+            for (int qb = 0; qb < x.nr; qb++) {
+                const int j = x.sr[qb];
+                double d = -Kr;
+                bool skipped = false;
+                #pragma unroll 1
+                for (int q = 0; q < x.nr; q++) {
+                    if (!skipped && x.sr[q] == j) { skipped = true; continue; }
+                    d *= s.C[x.sr[q]];
+                }
+                #pragma unroll 1
+                for (int q = 0; q < x.nl; q++) { double& c = J[x.sl[q] * n + j]; c = c - d; }
+                #pragma unroll 1
+                for (int q = 0; q < x.nr; q++) { double& c = J[x.sr[q] * n + j]; c = c + d; }
+            }
+        }
+    }
+    // third-body columns, J_ij += nu_i w_t E_tj (JF* third-body block)
+    #pragma unroll 1
+    for (int e = 0; e < M.nTbInc; e++) {
+        const int v = __ldg(&M.tbInc[e]);
+        const int i = v >> 16, t = (v >> 1) & 0x7fff;
+        const double w = s.tbF[t];
+        const double* eff = M.eff + (size_t)t * ns;
+        LA<double> row = J + i * n;
+        if (v & 1) {
+            #pragma unroll 4
+            for (int j = 0; j < ns; j++) row[j] = row[j] + __ldg(&eff[j]) * w;
+        } else {
+            #pragma unroll 4
+            for (int j = 0; j < ns; j++) row[j] = row[j] - __ldg(&eff[j]) * w;
+        }
+    }
+    // rows: production rate, temperature column and the dC/dY conversion
+    // (diagonal scaling + rank-1 correction)
+    double dtd = 0, dd = 0;
+    #pragma unroll 1
+    for (int i = 0; i < ns; i++) {
+        LA<double> row = J + i * n;
+        const double w = f[i], tc = tcAcc[i];
+        const double WiByrhoM = invRhoM * __ldg(&M.W[i]);
+        const double dY = w * WiByrhoM;
+        double S = 0;
+        #pragma unroll 4
+        for (int k = 0; k < ns; k++) S = fma(row[k], s.C[k], S);
+        const double tcol = WiByrhoM * (tc - S * invT) + invT * dY;
+        if (fast) {
+            #pragma unroll 4
+            for (int j = 0; j < ns; j++) {
+                const double invWj = __ldg(&M.invW[j]);
+                row[j] = WiByrhoM * (row[j] * (rhoM * invWj)) + (MW * invWj) * dY;
+            }
+        } else {
+            const double K = dY - WiByrhoM * S;
+            const double Wi = __ldg(&M.W[i]);
+            #pragma unroll 4
+            for (int j = 0; j < ns; j++) {
+                const double invWj = __ldg(&M.invW[j]);
+                row[j] = fma(row[j], Wi * invWj, (MW * invWj) * K);
+            }
+        }
+        row[ns] = tcol;
+        f[i] = dY;
+        dtd = fma(s.Ha[i], dY, dtd);
+        dd += dY * s.Cp[i] + tcol * s.Ha[i];
+    }
+    const double dTdt = -dtd / CpM;
+    // temperature row (ddTdtdYT)
+    #pragma unroll 1
+    for (int j = 0; j < ns; j++) {
+        double v = 0;
+        #pragma unroll 4
+        for (int i = 0; i < ns; i++) v -= J[i * n + j] * s.Ha[i];
+        v -= s.Cp[j] * dTdt;
+        J[ns * n + j] = v / CpM;
+    }
+    J[ns * n + ns] = (-dd - dTdt * dCpMdT) / CpM;
+    f[ns] = dTdt;
+}
+
+// ------------------------------------------------------------------------
+// linear algebra of one attempt, per lane
+
+// FP64: A = c I - J in place
+__device__ __noinline__ void lane_form_iteration(LA<double> A, int n, double c) {
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) {
+        LA<double> row = A + i * n;
+        #pragma unroll 4
+        for (int j = 0; j < n; j++) row[j] = -row[j];
+        row[i] = row[i] + c;
+    }
+}
+
+// choose_pivot (LUsolver.C:106-246 panel rules) over a per-lane matrix
+__device__ __forceinline__ int lane_choose_pivot(const LA<double>& A, int n, int k, int pos, int size) {
+    const int cand = size - pos;
+    if (cand <= 1) return k;
+    if (pos == 0 && size >= 3) {
+        int best = 0;
+        double t = 0;
+        #pragma unroll 1
+        for (int c = 0; c < size; c++) {
+            const double v = fabs(A[(k + c) * n + k]);
+            if (t < v) { best = c; t = v; }
+        }
+        return k + best;
+    }
+    if (size == 4 && pos == 1) {
+        // LUsolver.C:169-185: the running maximum keeps the signed value of row 2
+        double t = fabs(A[k * n + k]);
+        int best = 0;
+        const double v1 = A[(k + 1) * n + k];
+        if (t < fabs(v1)) { best = 1; t = v1; }
+        if (t < fabs(A[(k + 2) * n + k])) best = 2;
+        return k + best;
+    }
+    return (fabs(A[k * n + k]) < fabs(A[(k + 1) * n + k])) ? k + 1 : k;
+}
+
+// LU with the reference's panel-local pivoting (LUsolver.C:106-246,
+// 503-660, 3058-3143), blocked by panels of four columns: the panel's
+// columns are factored and updated eagerly, the panel's U rows and the
+// trailing block receive the panel's rank-4 update afterwards, each element
+// in the same multiply-add order as the column-by-column factorisation.
+__device__ __noinline__ void lane_lu(LA<double> A, int n, LA<int> piv, LA<double> invD) {
+    const int rem = n & 3;
+    int k0 = 0;
+    #pragma unroll 1
+    while (k0 < n) {
+        const bool tail = k0 >= n - rem;
+        const int size = tail ? rem : 4;
+        if (size == 1) {
+            invD[k0] = 1.0 / A[k0 * n + k0];
+            piv[k0] = k0;
+            break;
+        }
+        const int k1 = k0 + size;
+        // (a) the panel's columns
+        #pragma unroll 1
+        for (int k = k0; k < k1; k++) {
+            const int pos = k - k0;
+            const int pr = lane_choose_pivot(A, n, k, pos, size);
+            double akk = A[pr * n + k];
+            if (akk == 0) akk = kPivEps;
+            const double rinv = 1.0 / akk;
+            invD[k] = rinv;
+            piv[k] = pr;
+            if (pr != k) {
+                LA<double> rk = A + k * n, rp = A + pr * n;
+                #pragma unroll 4
+                for (int j = 0; j < n; j++) { const double t = rk[j]; rk[j] = rp[j]; rp[j] = t; }
+            }
+            #pragma unroll 4
+            for (int i = k + 1; i < n; i++) A[i * n + k] = A[i * n + k] * rinv;
+            if (k + 1 < k1) {
+                #pragma unroll 1
+                for (int i = k + 1; i < n; i++) {
+                    const double l = A[i * n + k];
+                    #pragma unroll 1
+                    for (int j = k + 1; j < k1; j++) A[i * n + j] = fma(-l, A[k * n + j], A[i * n + j]);
+                }
+            }
+        }
+        if (k1 >= n) break;
+        // (b) the panel's U rows in the trailing columns
+        #pragma unroll 1
+        for (int k = k0 + 1; k < k1; k++) {
+            #pragma unroll 1
+            for (int m = k0; m < k; m++) {
+                const double l = A[k * n + m];
+                LA<double> rk = A + k * n, rm = A + m * n;
+                #pragma unroll 4
+                for (int j = k1; j < n; j++) rk[j] = fma(-l, rm[j], rk[j]);
+            }
+        }
+        // (c) the trailing block: A[i][j] -= sum over the panel's m, in order
+        const LA<double> u0 = A + k0 * n, u1 = A + (k0 + 1) * n;
+        if (size == 4) {
+            const LA<double> u2 = A + (k0 + 2) * n, u3 = A + (k0 + 3) * n;
+            #pragma unroll 1
+            for (int i = k1; i < n; i++) {
+                LA<double> ri = A + i * n;
+                const double l0 = ri[k0], l1 = ri[k0 + 1], l2 = ri[k0 + 2], l3 = ri[k0 + 3];
+                #pragma unroll 2
+                for (int j = k1; j < n; j++) {
+                    double a = ri[j];
+                    a = fma(-l0, u0[j], a);
+                    a = fma(-l1, u1[j], a);
+                    a = fma(-l2, u2[j], a);
+                    a = fma(-l3, u3[j], a);
+                    ri[j] = a;
+                }
+            }
+        } else {
+            #pragma unroll 1
+            for (int i = k1; i < n; i++) {
+                LA<double> ri = A + i * n;
+                const double l0 = ri[k0], l1 = ri[k0 + 1];
+                const double l2 = size == 3 ? ri[k0 + 2] : 0.0;
+                const LA<double> u2 = A + (k0 + (size == 3 ? 2 : 1)) * n;
+                #pragma unroll 1
+                for (int j = k1; j < n; j++) {
+                    double a = ri[j];
+                    a = fma(-l0, u0[j], a);
+                    a = fma(-l1, u1[j], a);
+                    if (size == 3) a = fma(-l2, u2[j], a);
+                    ri[j] = a;
+                }
+            }
+        }
+        k0 = k1;
+    }
+}
+
+// Forward / back substitution with the factors of lane_lu (LUsolver.C:3145-3171,
+// 4113-4152): the recorded interchanges, unit-lower forward sweep, upper
+// backward sweep times the reciprocal pivots; in place on b.
+template<class VT>
+__device__ __noinline__ void lane_lu_solve(const LA<double> A, int n, const LA<int> piv, const LA<double> invD,
+                                           LA<VT> b) {
+    #pragma unroll 1
+    for (int j = 0; j < n; j++) {
+        const int p = piv[j];
+        if (p != j) { const VT t = b[j]; b[j] = b[p]; b[p] = t; }
+    }
+    #pragma unroll 1
+    for (int i = 1; i < n; i++) {
+        const LA<double> ri = A + i * n;
+        VT acc = b[i];
+        #pragma unroll 4
+        for (int j = 0; j < i; j++) acc = fma(-VT(ri[j]), b[j], acc);
+        b[i] = acc;
+    }
+    #pragma unroll 1
+    for (int i = n - 1; i >= 0; i--) {
+        const LA<double> ri = A + i * n;
+        VT acc = b[i];
+        #pragma unroll 4
+        for (int j = n - 1; j > i; j--) acc = fma(-VT(ri[j]), b[j], acc);
+        b[i] = acc * VT(invD[i]);
+    }
+}
+
+// ------------------------------------------------------------------------
+// Rosenbrock attempts, per lane (same stage arithmetic as fcs_kernels.cuh).
+// Vectors: 0 y0, 1 yTemp, 2..6 k1..k5, 7 dy, 8 err, 9 dydx, 10 dfdx, 11 tmp, 12 tcAcc
+
+__device__ __forceinline__ void lane_jacobian_and_lu(const DevMech& M, const KOpts& o, const LaneSlot& s, double p,
+                                                     double cdiag) {
+    lane_jac(M, s, p, s.v(0), s.v(10), s.A, s.v(12), o.jacobian);
+    lane_form_iteration(s.A, M.n, cdiag);
+    lane_lu(s.A, M.n, s.piv, s.invD);
+}
+
+__device__ __forceinline__ void lane_solve(const LaneSlot& s, int n, LA<double> b) {
+    lane_lu_solve<double>(s.A, n, s.piv, s.invD, b);
+}
+
+__device__ __forceinline__ double lane_err_norm(const KOpts& o, int n, const LA<double>& y0, const LA<double>& yt,
+                                                const LA<double>& err) {
+    double me = 0;
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) {
+        const double tol = o.absTol + o.relTol * fmax(fabs(y0[i]), fabs(yt[i]));
+        const double e = fabs(err[i]) / tol;
+        me = (e > me || e != e) ? e : me;
+    }
+    return me;
+}
+
+// OptRodas34::Rodas34Solve (OptRodas34.C:291-882), constants OptRodas34.H:105-149
+__device__ __noinline__ double lane_rodas34(const DevMech& M, const KOpts& o, const LaneSlot& s, double p, double dx,
+                                            double invdx, CellCounters& cc) {
+    const int n = M.n;
+    const LA<double> y0 = s.v(0), yTemp = s.v(1), k1 = s.v(2), k2 = s.v(3), k3 = s.v(4), k4 = s.v(5);
+    const LA<double> k5 = s.v(6), dy = s.v(7), err = s.v(8), dydx = s.v(9), dfdx = s.v(10);
+    const double d1 = 0.25, d2 = -0.1043, d3 = 0.1035, d4 = -0.3620000000000023e-01;
+    const double a21 = 0.1544e1, a31 = 0.9466785280815826, a32 = 0.2557011698983284;
+    const double a41 = 0.3314825187068521e1, a42 = 0.2896124015972201e1, a43 = 0.9986419139977817;
+    const double a51 = 0.1221224509226641e1, a52 = 0.6019134481288629e1, a53 = 0.1253708332932087e2,
+                 a54 = -0.6878860361058950;
+    const double c21 = -0.56688e1, c31 = -0.2430093356833875e1, c32 = -0.2063599157091915;
+    const double c41 = -0.1073529058151375, c42 = -0.9594562251023355e1, c43 = -0.2047028614809616e2;
+    const double c51 = 0.7496443313967647e1, c52 = -0.1024680431464352e2, c53 = -0.3399990352819905e2,
+                 c54 = 0.1170890893206160e2;
+    const double c61 = 0.8083246795921522e1, c62 = -0.7981132988064893e1, c63 = -0.3152159432874371e2,
+                 c64 = 0.1631930543123136e2, c65 = -0.6058818238834054e1;
+    const double invgamma = 1.0 / 0.25;
+    const double cdiag = 1.0 * invdx * invgamma;
+    lane_jacobian_and_lu(M, o, s, p, cdiag);
+    cc.jac++; cc.lu++; cc.rhs += 5; cc.solves += 6;
+
+    const double dxd1 = dx * d1 + 1;
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) k1[i] = dxd1 * dfdx[i];
+    lane_solve(s, n, k1);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) yTemp[i] = fma(a21, k1[i], y0[i]);
+    lane_rhs(M, s, p, yTemp, dydx, 1);
+    {
+        const double dxd2 = dx * d2, e1 = c21 * invdx;
+        #pragma unroll 1
+        for (int i = 0; i < n; i++) k2[i] = fma(e1, k1[i], fma(dxd2, dfdx[i], dydx[i]));
+    }
+    lane_solve(s, n, k2);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) yTemp[i] = fma(a32, k2[i], fma(a31, k1[i], y0[i]));
+    lane_rhs(M, s, p, yTemp, dydx, 1);
+    {
+        const double dxd3 = dx * d3, e1 = c31 * invdx, e2 = c32 * invdx;
+        #pragma unroll 1
+        for (int i = 0; i < n; i++) k3[i] = fma(e2, k2[i], fma(e1, k1[i], fma(dxd3, dfdx[i], dydx[i])));
+    }
+    lane_solve(s, n, k3);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) yTemp[i] = fma(a43, k3[i], fma(a42, k2[i], fma(a41, k1[i], y0[i])));
+    lane_rhs(M, s, p, yTemp, dydx, 1);
+    {
+        const double dxd4 = dx * d4, e1 = c41 * invdx, e2 = c42 * invdx, e3 = c43 * invdx;
+        #pragma unroll 1
+        for (int i = 0; i < n; i++)
+            k4[i] = fma(e3, k3[i], fma(e2, k2[i], fma(e1, k1[i], fma(dxd4, dfdx[i], dydx[i]))));
+    }
+    lane_solve(s, n, k4);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) {
+        const double d = fma(a54, k4[i], fma(a53, k3[i], fma(a52, k2[i], a51 * k1[i])));
+        dy[i] = d;
+        yTemp[i] = y0[i] + d;
+    }
+    lane_rhs(M, s, p, yTemp, dydx, 1);
+    {
+        const double e1 = c51 * invdx, e2 = c52 * invdx, e3 = c53 * invdx, e4 = c54 * invdx;
+        #pragma unroll 1
+        for (int i = 0; i < n; i++) k5[i] = fma(e4, k4[i], fma(e3, k3[i], fma(e2, k2[i], fma(e1, k1[i], dydx[i]))));
+    }
+    lane_solve(s, n, k5);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) {
+        const double d = dy[i] + k5[i];
+        dy[i] = d;
+        yTemp[i] = y0[i] + d;
+    }
+    lane_rhs(M, s, p, yTemp, dydx, 2);
+    {
+        const double e1 = c61 * invdx, e2 = c62 * invdx, e3 = c63 * invdx, e4 = c64 * invdx, e5 = c65 * invdx;
+        #pragma unroll 1
+        for (int i = 0; i < n; i++)
+            err[i] = fma(e5, k5[i], fma(e4, k4[i], fma(e3, k3[i], fma(e2, k2[i], fma(e1, k1[i], dydx[i])))));
+    }
+    lane_solve(s, n, err);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) yTemp[i] = y0[i] + dy[i] + err[i];
+    return lane_err_norm(o, n, y0, yTemp, err);
+}
+
+// OptRosenbrock34::Rosenbrock34Solve (OptRosenbrock34.C:281-678), .H:127-158
+__device__ __noinline__ double lane_ros34(const DevMech& M, const KOpts& o, const LaneSlot& s, double p, double dx,
+                                          double invdx, CellCounters& cc) {
+    const int n = M.n;
+    const LA<double> y0 = s.v(0), yTemp = s.v(1), k1 = s.v(2), k2 = s.v(3), k3 = s.v(4), k4 = s.v(5);
+    const LA<double> err = s.v(8), dydx = s.v(9), dfdx = s.v(10);
+    const double a21 = 2, a31 = 48.0 / 25.0, a32 = 6.0 / 25.0;
+    const double c21 = -8, c31 = 372.0 / 25.0, c32 = 12.0 / 5.0;
+    const double c41 = -112.0 / 125.0, c42 = -54.0 / 125.0, c43 = -2.0 / 5.0;
+    const double b1 = 19.0 / 9.0, b2 = 1.0 / 2.0, b3 = 25.0 / 108.0, b4 = 125.0 / 108.0;
+    const double e1 = 34.0 / 108.0, e2 = 7.0 / 36.0, e4 = 125.0 / 108.0;
+    const double d1 = 1.0 / 2.0, d2 = -3.0 / 2.0, d3 = 605.0 / 250.0, d4 = 29.0 / 250.0;
+    const double invgamma = 1.0 / (1.0 / 2.0);
+    const double cdiag = invdx * invgamma;
+    lane_jacobian_and_lu(M, o, s, p, cdiag);
+    cc.jac++; cc.lu++; cc.rhs += 2; cc.solves += 4;
+
+    const double dxd1 = dx * d1 + 1;
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) k1[i] = dxd1 * dfdx[i];
+    lane_solve(s, n, k1);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) yTemp[i] = fma(a21, k1[i], y0[i]);
+    lane_rhs(M, s, p, yTemp, dydx, 1);
+    {
+        const double dxd2 = dx * d2, f1 = c21 * invdx;
+        #pragma unroll 1
+        for (int i = 0; i < n; i++) k2[i] = fma(f1, k1[i], fma(dxd2, dfdx[i], dydx[i]));
+    }
+    lane_solve(s, n, k2);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) yTemp[i] = fma(a32, k2[i], fma(a31, k1[i], y0[i]));
+    lane_rhs(M, s, p, yTemp, dydx, 1);
+    {
+        const double dxd3 = dx * d3, f1 = c31 * invdx, f2 = c32 * invdx;
+        #pragma unroll 1
+        for (int i = 0; i < n; i++) k3[i] = fma(f2, k2[i], fma(f1, k1[i], fma(dxd3, dfdx[i], dydx[i])));
+    }
+    lane_solve(s, n, k3);
+    {
+        const double dxd4 = dx * d4, f1 = c41 * invdx, f2 = c42 * invdx, f3 = c43 * invdx;
+        #pragma unroll 1
+        for (int i = 0; i < n; i++)
+            k4[i] = fma(f3, k3[i], fma(f2, k2[i], fma(f1, k1[i], fma(dxd4, dfdx[i], dydx[i]))));
+    }
+    lane_solve(s, n, k4);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) {
+        yTemp[i] = fma(b4, k4[i], fma(b3, k3[i], fma(b2, k2[i], fma(b1, k1[i], y0[i]))));
+        err[i] = fma(e4, k4[i], fma(e2, k2[i], e1 * k1[i]));
+    }
+    return lane_err_norm(o, n, y0, yTemp, err);
+}
+
+// OptRodas23::Rodas23Solve (OptRodas23.C:202-315), constants OptRodas23.H:113-126
+__device__ __noinline__ double lane_rodas23(const DevMech& M, const KOpts& o, const LaneSlot& s, double p, double dx,
+                                            double invdx, CellCounters& cc) {
+    const int n = M.n;
+    const LA<double> y0 = s.v(0), yTemp = s.v(1), k1 = s.v(2), k2 = s.v(3), k3 = s.v(4);
+    const LA<double> dy = s.v(7), err = s.v(8), dydx = s.v(9), dfdx = s.v(10);
+    const double d1 = 1.0 / 2.0, d2 = 3.0 / 2.0, a31 = 2, c21 = 4, c31 = 1, c32 = -1;
+    const double c41 = 1, c42 = -1, c43 = -8.0 / 3.0;
+    const double invgamma = 1.0 / (1.0 / 2.0);
+    const double cdiag = invdx * invgamma;
+    lane_jacobian_and_lu(M, o, s, p, cdiag);
+    cc.jac++; cc.lu++; cc.rhs += 2; cc.solves += 4;
+
+    const double dxd1 = dx * d1, dxd2 = dx * d2;
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) k1[i] = fma(dxd1, dfdx[i], dfdx[i]);
+    lane_solve(s, n, k1);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) k2[i] = fma(dxd2, dfdx[i], dfdx[i]) + c21 * k1[i] / dx;
+    lane_solve(s, n, k2);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) {
+        dy[i] = a31 * k1[i];
+        yTemp[i] = y0[i] + dy[i];
+    }
+    lane_rhs(M, s, p, yTemp, dydx, 1);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) k3[i] = dydx[i] + fma(c32, k2[i], c31 * k1[i]) / dx;
+    lane_solve(s, n, k3);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) {
+        dy[i] = dy[i] + k3[i];
+        yTemp[i] = y0[i] + dy[i];
+    }
+    lane_rhs(M, s, p, yTemp, dydx, 1);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) err[i] = dydx[i] + fma(c43, k3[i], fma(c42, k2[i], c41 * k1[i])) / dx;
+    lane_solve(s, n, err);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) yTemp[i] = y0[i] + dy[i] + err[i];
+    return lane_err_norm(o, n, y0, yTemp, err);
+}
+
+// OptRosenbrock23::Rosenbrock23Solve (OptRosenbrock23.C:208-298), constants .H:116-140
+__device__ __noinline__ double lane_ros23(const DevMech& M, const KOpts& o, const LaneSlot& s, double p, double dx,
+                                          double invdx, CellCounters& cc) {
+    const int n = M.n;
+    const LA<double> y0 = s.v(0), yTemp = s.v(1), k1 = s.v(2), k2 = s.v(3), k3 = s.v(4);
+    const LA<double> err = s.v(8), dydx = s.v(9), dfdx = s.v(10);
+    const double a21 = 1;
+    const double c21 = -1.0156171083877702091975600115545, c31 = 4.0759956452537699824805835358067;
+    const double c32 = 9.2076794298330791242156818474003;
+    const double b1 = 1, b2 = 6.1697947043828245592553615689730, b3 = -0.4277225654321857332623837380651;
+    const double e1 = 0.5, e2 = -2.9079558716805469821718236208017, e3 = 0.2235406989781156962736090927619;
+    const double gamma = 0.43586652150845899941601945119356, invgamma = 1.0 / gamma;
+    const double d1 = 0.43586652150845899941601945119356, d2 = 0.24291996454816804366592249683314;
+    const double d3 = 2.1851380027664058511513169485832;
+    const double cdiag = invdx * invgamma;
+    lane_jacobian_and_lu(M, o, s, p, cdiag);
+    cc.jac++; cc.lu++; cc.rhs += 1; cc.solves += 3;
+
+    const double dxd1 = dx * d1, dxd2 = dx * d2, dxd3 = dx * d3;
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) k1[i] = fma(dxd1, dfdx[i], dfdx[i]);
+    lane_solve(s, n, k1);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) yTemp[i] = fma(a21, k1[i], y0[i]);
+    lane_rhs(M, s, p, yTemp, dydx, 1);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) k2[i] = fma(dxd2, dfdx[i], dydx[i]) + c21 * k1[i] / dx;
+    lane_solve(s, n, k2);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) k3[i] = fma(dxd3, dfdx[i], dydx[i]) + fma(c32, k2[i], c31 * k1[i]) / dx;
+    lane_solve(s, n, k3);
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) {
+        yTemp[i] = fma(b3, k3[i], fma(b2, k2[i], fma(b1, k1[i], y0[i])));
+        err[i] = fma(e3, k3[i], fma(e2, k2[i], e1 * k1[i]));
+    }
+    return lane_err_norm(o, n, y0, yTemp, err);
+}
+
+__device__ __forceinline__ double lane_attempt(const DevMech& M, const KOpts& o, const LaneSlot& s, double p,
+                                               double dx, CellCounters& cc) {
+    const double invdx = 1.0 / dx;
+    switch (o.solver) {
+        case FCS_SOLVER_ROSENBROCK34: return lane_ros34(M, o, s, p, dx, invdx, cc);
+        case FCS_SOLVER_RODAS23: return lane_rodas23(M, o, s, p, dx, invdx, cc);
+        case FCS_SOLVER_ROSENBROCK23: return lane_ros23(M, o, s, p, dx, invdx, cc);
+        default: return lane_rodas34(M, o, s, p, dx, invdx, cc);
+    }
+}
+
+// ------------------------------------------------------------------------
+// the kernel
+
+// Per-lane state of the step-size controller (ODESolve + adaptiveSolve,
+// OptRodas34.C:123-289), kept across loop iterations so that every lane runs
+// one attempt per iteration whatever its cell's progress.
+struct LaneCtl {
+    long long c;      // cell, or -1
+    double p, deltaT, x, dxTry, dxTry0, dx;
+    double sub0;      // the cell's initial sub-step (kept on failure, as ODESolve leaves it)
+    int nStep, rejects;
+    bool last, retry;
+};
+
+template<class MT>
+__global__ void __launch_bounds__(128, 4)
+lane_integrate_kernel(const DevMech M, const KOpts o, const LaneLayout L, CellIO io, WorkQueue q,
+                      double* __restrict__ ws) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const long long gwarp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const LaneSlot s = make_lane_slot(ws + (size_t)gwarp * L.words * kLanes, L);
+    const int ns = M.ns, n = M.n;
+    const long long nc = io.nCells;
+    const double SAFE = 0.9, ALPHA_INC = 0.2, ALPHA_DEC = 0.25, MIN_SCALE = 0.2, MAX_SCALE = 10;
+    const double ratio = 5.904900000000001e-06;  // (MAX_SCALE/SAFE)^(-1/ALPHA_INC)
+    const double safeMaxScale = SAFE * MAX_SCALE;
+    const int qn = q.nDev ? *q.nDev : q.n;
+    const LA<double> y = s.v(0), yTemp = s.v(1);
+    CellCounters cc;
+    long long nCells = 0, nFailed = 0;
+    double dtMin = 1e300;
+    LaneCtl k;
+    k.c = -1;
+    bool exhausted = false;
+    for (;;) {
+        // 1. lanes without a cell take the next ones from the queue
+        const bool want = k.c < 0 && !exhausted;
+        const unsigned m = __ballot_sync(FULL, want);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(q.head, __popc(m));
+            base = __shfl_sync(FULL, base, leader);
+            if (want) {
+                const int idx = base + __popc(m & ((1u << lane) - 1));
+                if (idx >= qn) {
+                    exhausted = true;
+                } else {
+                    const long long c = q.order ? q.order[idx] : idx;
+                    k.c = c;
+                    k.p = io.p[c];
+                    k.deltaT = io.dtPerCell ? io.dtPerCell[c] : io.deltaT;
+                    #pragma unroll 1
+                    for (int i = 0; i < ns; i++) {
+                        const double Yi = io.Y[(size_t)i * nc + c];
+                        y[i] = Yi > 0 ? Yi : 0.0;
+                    }
+                    y[ns] = io.T[c];
+                    k.x = 0;
+                    k.sub0 = io.subDt[c];
+                    k.dxTry = k.sub0;
+                    k.nStep = 0;
+                    k.last = false;
+                    k.retry = false;
+                }
+            }
+        }
+        if (!__any_sync(FULL, k.c >= 0)) break;
+        int st = -1;  // >= 0: the lane's cell finishes with this status
+        if (k.c >= 0) {
+            if (!(k.deltaT > kSmall)) {
+                st = FCS_CELL_OK;  // nothing to integrate (transientSolve.H's loop does not run)
+            } else {
+                // 2. the step size of this attempt
+                if (!k.retry) {
+                    k.dxTry0 = k.dxTry;
+                    if ((k.x + k.dxTry - k.deltaT) * (k.x + k.dxTry - 0.0) > 0) {
+                        k.last = true;
+                        k.dxTry = k.deltaT - k.x;
+                    }
+                    k.dx = k.dxTry;
+                    k.rejects = 0;
+                }
+                // 3. one attempt (the same code on every lane)
+                const double Err = lane_attempt(M, o, s, k.p, k.dx, cc);
+                cc.attempts++;
+                // 4. the controller
+                if (Err > 1) {
+                    if (++k.rejects > o.maxRejects) {
+                        st = FCS_CELL_DT_UNDERFLOW;
+                    } else {
+                        k.dx *= fmax(SAFE * pow(Err, -ALPHA_DEC), MIN_SCALE);
+                        k.retry = true;
+                    }
+                } else if (!(Err == Err)) {
+                    st = FCS_CELL_NONFINITE;
+                } else {
+                    cc.accepted++;
+                    k.retry = false;
+                    k.x += k.dx;
+                    #pragma unroll 1
+                    for (int i = 0; i < n; i++) y[i] = yTemp[i];
+                    k.dxTry = (Err > ratio) ? fmin(fmax(SAFE * pow(Err, -ALPHA_INC), MIN_SCALE), MAX_SCALE) * k.dx
+                                            : safeMaxScale * k.dx;
+                    if ((k.x - k.deltaT) * (k.deltaT - 0.0) >= 0) {
+                        if (k.nStep > 0 && k.last) k.dxTry = k.dxTry0;
+                        st = FCS_CELL_OK;
+                    } else if (++k.nStep >= o.maxSteps) {
+                        st = FCS_CELL_MAX_STEPS;
+                    }
+                }
+            }
+        }
+        // 5. a finished cell writes its results and frees the lane
+        if (st >= 0) {
+            const long long c = k.c;
+            nCells++;
+            if (st != FCS_CELL_OK) nFailed++;
+            const double rho0 = io.rho0[c];
+            #pragma unroll 1
+            for (int i = 0; i < ns; i++) {
+                const double Yn = y[i] > 0 ? y[i] : 0.0;
+                const size_t a = (size_t)i * nc + c;
+                const double Y0 = io.Y[a];
+                if (io.RR) io.RR[a] = (Yn * rho0 - Y0 * rho0) / k.deltaT;
+                io.Y[a] = Yn;
+            }
+            io.T[c] = y[ns];
+            const double subDt = st == FCS_CELL_OK ? k.dxTry : k.sub0;
+            dtMin = fmin(dtMin, subDt);
+            io.subDt[c] = subDt < o.dtChemMax ? subDt : o.dtChemMax;
+            if (io.status) io.status[c] = st;
+            k.c = -1;
+        }
+    }
+    // every lane leaves the loop in the same iteration: warp sums, one atomic per warp
+    long long v[ST_COUNT] = {};
+    v[ST_CELLS] = nCells; v[ST_FAILED] = nFailed; v[ST_ATTEMPTS] = cc.attempts; v[ST_ACCEPTED] = cc.accepted;
+    v[ST_JAC] = cc.jac; v[ST_LU] = cc.lu; v[ST_RHS] = cc.rhs; v[ST_SOLVES] = cc.solves;
+    v[ST_FALLBACK] = cc.fallbacks;
+    unsigned long long dm = nCells ? dbits(dtMin) : ~0ull;
+    #pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        #pragma unroll
+        for (int t = 0; t < ST_COUNT; t++) v[t] += __shfl_down_sync(FULL, v[t], off);
+        const unsigned long long u = __shfl_down_sync(FULL, dm, off);
+        dm = u < dm ? u : dm;
+    }
+    if (lane == 0) {
+        #pragma unroll
+        for (int t = 0; t < ST_COUNT; t++)
+            if (t != ST_SKIPPED && v[t]) atomicAdd(reinterpret_cast<unsigned long long*>(&io.stats[t]),
+                                                   (unsigned long long)v[t]);
+        if (v[ST_CELLS]) atomicMin(io.dtMinBits, dm);
+    }
+}
+
+}  // namespace fcs

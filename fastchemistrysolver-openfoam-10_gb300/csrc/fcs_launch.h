@@ -38,7 +38,7 @@ enum { QC_HEAD = 0, QC_LEN = 1, QC_BINS = 2, QC_FILL = QC_BINS + kQueueBins, QC_
        QC_COUNT };
 
 struct LaunchCfg {
-    int group;                 // threads per cell: 32, 64, 128, 256
+    int group;                 // threads per cell: 32, 64, 128, 256, or 1 (lane per cell)
     int block;                 // threads per block
     int grid;                  // blocks
 };
@@ -60,6 +60,13 @@ cudaError_t launch_classify_binned(const CellIO& io, int ns, double Treact, int*
                                    cudaStream_t st);
 // order[] = cells with bin >= 0, highest bin first; counters[QC_LEN] = their count.
 cudaError_t launch_queue(long long nc, const int* bin, int* counters, int* order, cudaStream_t st);
+
+// The lane-per-cell integrator (fcs_lane.cu): lc.group == 1, lc.block
+// threads per block, one cell per thread; gws holds make_lane_layout(...).words
+// doubles per thread of the grid.
+cudaError_t launch_lane_integrate(const LaunchCfg& lc, bool mixed, const DevMech& M, const KOpts& o,
+                                  const CellIO& io, const WorkQueue& q, char* gws, cudaStream_t st);
+cudaError_t lane_attributes(bool mixed, int* maxThreads, int* regs);
 
 // per-group-size instantiations (fcs_kernels_g<G>.cu)
 template<int G>

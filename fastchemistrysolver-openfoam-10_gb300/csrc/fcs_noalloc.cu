@@ -61,32 +61,17 @@ fcs_status scratch_base(fcs_ctx* ctx, unsigned char** out) {
     return FCS_OK;
 }
 
-// A cell array must be device (or managed) memory of this context's device,
-// 8-byte aligned: host memory handed to a kernel would fault.
-fcs_status check_device_array(fcs_ctx* ctx, const void* ptr, const char* name, size_t align) {
-    if (reinterpret_cast<uintptr_t>(ptr) % align != 0)
-        return set_err(ctx, FCS_ERR_INVALID, std::string(name) + " is not aligned");
-    cudaPointerAttributes a{};
-    const cudaError_t e = cudaPointerGetAttributes(&a, ptr);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return set_err(ctx, FCS_ERR_INVALID, std::string(name) + " is not a device pointer");
-    }
-    const bool ok = (a.type == cudaMemoryTypeDevice && a.device == ctx->device) || a.type == cudaMemoryTypeManaged;
-    if (!ok)
-        return set_err(ctx, FCS_ERR_INVALID,
-                       std::string(name) + " must be device memory of the context's device (fcs_integrate takes host arrays)");
-    return FCS_OK;
-}
-
 }  // namespace
 
 extern "C" fcs_status fcs_integrate_noalloc(fcs_ctx* ctx, int64_t nc, double dt, const double* p,
                                             const double* rho0, double* T, double* Y, double* sub,
                                             double* RR, int32_t* status, fcs_step_stats* stats,
                                             double* dtMin) {
+    fcs_status s0;
     if (!ctx) return FCS_ERR_INVALID;
     if (!ctx->loaded) return set_err(ctx, FCS_ERR_STATE, "no mechanism loaded");
+    // a pending asynchronous step still reads the context's events and stream
+    if ((s0 = refuse_if_async_pending(ctx)) != FCS_OK) return s0;
     if (nc < 0 || nc > kMaxCells)
         return set_err(ctx, FCS_ERR_INVALID,
                        "n_cells out of range: fcs_integrate_noalloc takes at most " +

@@ -25,13 +25,14 @@ CUDA_GRAPH = 4
 
 CELL_STATUS = {0: "ok", 1: "max_steps", 2: "nonfinite", 3: "dt_underflow", 4: "skipped"}
 ERRORS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "STATE", 5: "CELLS", 6: "UNSUPPORTED",
-          7: "PARSE"}
+          7: "PARSE", 8: "TIMEOUT"}
 
 EXPORTS = ("fcs_create", "fcs_destroy", "fcs_last_error_string", "fcs_version", "fcs_load_mechanism",
            "fcs_load_mechanism_foam", "fcs_parse_mechanism_foam", "fcs_read_chemistry_properties",
            "fcs_default_options",
            "fcs_set_options", "fcs_mechanism_size", "fcs_integrate", "fcs_integrate_lts",
-           "fcs_integrate_noalloc", "fcs_integrate_async", "fcs_sync", "fcs_rhs", "fcs_tc",
+           "fcs_integrate_noalloc", "fcs_integrate_async", "fcs_sync", "fcs_sync_timeout",
+           "fcs_test_fail_allocations", "fcs_rhs", "fcs_tc",
            "fcs_jacobian", "fcs_rates", "fcs_bench_fp64_peak", "fcs_bench_fp32_peak", "fcs_check_exp",
            # include/fcs_mlp.h
            "fcs_mlp_create", "fcs_mlp_destroy", "fcs_mlp_last_error", "fcs_mlp_get_shape", "fcs_mlp_param_count",
@@ -128,6 +129,8 @@ def load(path: str = LIB) -> C.CDLL:
     L.fcs_integrate_noalloc.argtypes = cell_args[:-1]
     L.fcs_integrate_async.argtypes = [vp, C.c_int64, C.c_double] + [vp] * 7 + [C.c_int32, vp]
     L.fcs_sync.argtypes = [vp, C.POINTER(StepStats), _dp]
+    L.fcs_sync_timeout.argtypes = [vp, C.c_double, C.POINTER(StepStats), _dp]
+    L.fcs_test_fail_allocations.argtypes = [C.c_int32]
     L.fcs_rhs.argtypes = [vp, C.c_int64, vp, vp, vp, vp, C.c_int32]
     L.fcs_jacobian.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, C.c_int32]
     L.fcs_rates.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, vp, C.c_int32]
@@ -207,6 +210,14 @@ def make_desc(flat) -> MechDesc:
     d.plog_offset = p(flat.plog_offset, C.c_int32); d.plog_table = p(flat.plog_table, C.c_double)
     d._keep = keep
     return d
+
+
+def fail_allocations(count: int) -> None:
+    """Test hook: the next `count` device-buffer growths of the library fail
+    (host side; fcs_test_fail_allocations)."""
+    st = load().fcs_test_fail_allocations(int(count))
+    if st:
+        raise FcsError(st, "fcs_test_fail_allocations")
 
 
 def fp64_peak_tflops(device: int = 0, ms: float = 50.0) -> float:
@@ -371,11 +382,16 @@ class Context:
                                         None if stream is None else stream.cuda_stream)
         self._check(st)
 
-    def sync(self, check=True):
+    def sync(self, check=True, timeout_ms=None):
+        """fcs_sync, or fcs_sync_timeout when timeout_ms is given (which may
+        return code 8, TIMEOUT, with the step still in flight)."""
         stats = StepStats()
         dmin = C.c_double(0)
-        st = self.L.fcs_sync(self.h, C.byref(stats), C.byref(dmin))
-        if check and st not in (0, 5):
+        if timeout_ms is None:
+            st = self.L.fcs_sync(self.h, C.byref(stats), C.byref(dmin))
+        else:
+            st = self.L.fcs_sync_timeout(self.h, float(timeout_ms), C.byref(stats), C.byref(dmin))
+        if check and st not in (0, 5, 8):
             self._check(st)
         return st, stats.as_dict(), dmin.value
 

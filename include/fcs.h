@@ -31,6 +31,8 @@
  *   - Species-major layout: Y[i * n_cells + c] is species i of cell c (one
  *     contiguous OpenFOAM field per species).
  *   - One context per host thread; calls on one context are serialised.
+ *     While a step of fcs_integrate_async is in flight, the entry points that
+ *     use the context's buffers return FCS_ERR_STATE until fcs_sync.
  */
 #ifndef FCS_H
 #define FCS_H
@@ -53,7 +55,8 @@ enum {
     FCS_ERR_STATE = 4,        /* call out of order (e.g. no mechanism loaded) */
     FCS_ERR_CELLS = 5,        /* some cells failed; see cell_status           */
     FCS_ERR_UNSUPPORTED = 6,  /* reaction type or size not supported          */
-    FCS_ERR_PARSE = 7         /* OpenFOAM dictionary could not be read        */
+    FCS_ERR_PARSE = 7,        /* OpenFOAM dictionary could not be read        */
+    FCS_ERR_TIMEOUT = 8       /* fcs_sync_timeout: the step is still running  */
 };
 
 /* Per-cell status codes (cell_status output). */
@@ -89,8 +92,12 @@ enum { FCS_JACOBIAN_EXACT = 0, FCS_JACOBIAN_FAST = 1 };
  * small is redone in FP64.  Rates, thermo, equilibrium constants, the
  * Jacobian assembly, state and the step controller stay FP64. */
 enum { FCS_PRECISION_FP64 = 0, FCS_PRECISION_MIXED = 1 };
-/* Cell-to-thread mapping: AUTO lets the autotuner choose. */
-enum { FCS_MAPPING_AUTO = 0, FCS_MAPPING_WARP = 32, FCS_MAPPING_BLOCK64 = 64,
+/* Cell-to-thread mapping: AUTO lets the autotuner choose.  LANE: one thread
+ * per cell, the cells' working sets in a global-memory workspace interleaved
+ * across the lanes of a warp (Rosenbrock-family solvers in FP64); the others:
+ * a group of 32..256 threads per cell with its working set in shared memory
+ * (or in global memory when it does not fit). */
+enum { FCS_MAPPING_AUTO = 0, FCS_MAPPING_LANE = 1, FCS_MAPPING_WARP = 32, FCS_MAPPING_BLOCK64 = 64,
        FCS_MAPPING_BLOCK128 = 128, FCS_MAPPING_BLOCK256 = 256 };
 
 /* flags for fcs_integrate */
@@ -262,6 +269,17 @@ fcs_status fcs_integrate_async(fcs_ctx* ctx, int64_t n_cells, double delta_t,
                                void* cuda_stream);
 fcs_status fcs_sync(fcs_ctx* ctx, fcs_step_stats* stats, double* delta_t_min);
 
+/*
+ * fcs_sync with a bounded host-side wait (no counterpart in the reference,
+ * whose only failure path is the fatal maxSteps, OptRodas34.C:193): waits at
+ * most timeout_ms for the step of fcs_integrate_async.  If the step has not
+ * completed by then it returns FCS_ERR_TIMEOUT and the step stays in flight
+ * (the kernels are not interrupted); a later fcs_sync or fcs_sync_timeout
+ * collects it.  While a step is in flight every other entry point that uses
+ * the context's buffers returns FCS_ERR_STATE.
+ */
+fcs_status fcs_sync_timeout(fcs_ctx* ctx, double timeout_ms, fcs_step_stats* stats, double* delta_t_min);
+
 /* Same, with a per-cell delta_t (the local-time-stepping variant
  * FastChemistryModel::solve(const scalarField& deltaT),
  * FastChemistryModel_localEulerSolve.H:3-101). */
@@ -305,11 +323,26 @@ fcs_status fcs_integrate_lts(fcs_ctx* ctx, int64_t n_cells, const double* delta_
  *     this library's device code); make it before any stream capture begins.
  */
 #define FCS_NOALLOC_MAX_CELLS 1048576
+/* (continued) The first launch of each kernel variant (mapping x precision x
+ * solver family) in a process may make the CUDA driver enlarge the
+ * context's local-memory reservation for the kernel's stack frame.  Make one
+ * call for each mapping and precision the run will use before the flow
+ * solver's pool takes the remaining device memory. */
 fcs_status fcs_integrate_noalloc(fcs_ctx* ctx, int64_t n_cells, double delta_t,
                                  const double* p, const double* rho0,
                                  double* T, double* Y, double* sub_delta_t,
                                  double* RR, int32_t* cell_status,
                                  fcs_step_stats* stats, double* delta_t_min);
+
+/*
+ * Test hook (host side only; no counterpart in the reference): the next
+ * `count` growths of the library's device buffers, in any context of this
+ * process, fail as if cudaMalloc had returned cudaErrorMemoryAllocation.  The
+ * entry point that needed the buffer returns FCS_ERR_NOMEM; the mechanism,
+ * the options and the other buffers stay as they were, and the next call
+ * allocates again.  0 clears it.
+ */
+fcs_status fcs_test_fail_allocations(int32_t count);
 
 /*
  * Right-hand side of the mass-fraction ODE system at each cell state:

@@ -1,9 +1,12 @@
 """fcs_integrate_noalloc (the entry point that allocates no device memory)
 against fcs_integrate on the same device arrays, through the C ABI.
 
-Both entry points run the same classify and integrate kernels with the same
-cell-to-thread mapping on the same cells, so the results agree to rounding of
-identical arithmetic: the test allows 1e-13 relative.  The file is named to be
+Both entry points run the same classify kernel (natural cell order:
+fcs_integrate is given FCS_NO_QUEUE_SORT) and the same integrate kernel with
+the same cell-to-thread mapping on the same cells, so the results agree to
+rounding of identical arithmetic: the test allows 1e-13 relative.  On each
+call the no-allocation entry point runs first, so in a fresh process the
+first launch of the integrate kernel is its own.  The file is named to be
 collected last, and passes alone in a fresh process as well.
 """
 import numpy as np
@@ -14,6 +17,7 @@ import fcs
 pytestmark = pytest.mark.gpu
 
 FCS_ERR_INVALID = 1
+FCS_NO_QUEUE_SORT = 2
 NOALLOC_MAX_CELLS = 1048576
 RTOL = 1e-13
 
@@ -51,16 +55,17 @@ def test_noalloc_matches_integrate_on_two_calls_in_a_row(built):
     ctx.set_options(abs_tol=w.abs_tol, rel_tol=w.rel_tol, mapping=64, treact=treact)
     a, b = _device_state(c), _device_state(c)
     for call in range(2):
-        code_a, stats_a, dmin_a = ctx.integrate_raw(c.n, w.dt, a["p"], a["rho0"], a["T"], a["Y"], a["subDt"],
-                                                    a["RR"], a["status"], device=True)
         torch.cuda.synchronize()
         free_before = torch.cuda.mem_get_info()[0]
         code_b, stats_b, dmin_b = ctx.integrate_noalloc(c.n, w.dt, b["p"], b["rho0"], b["T"], b["Y"], b["subDt"],
                                                         b["RR"], b["status"])
         torch.cuda.synchronize()
         free_after = torch.cuda.mem_get_info()[0]
+        code_a, stats_a, dmin_a = ctx.integrate_raw(c.n, w.dt, a["p"], a["rho0"], a["T"], a["Y"], a["subDt"],
+                                                    a["RR"], a["status"], device=True, flags=FCS_NO_QUEUE_SORT)
+        torch.cuda.synchronize()
         assert code_a == 0 and code_b == 0, (code_a, code_b, ctx.last_error())
-        if call == 1:  # the first call may load the scratch's device module
+        if call == 1:  # the first call may load the scratch's device module and grow the stack reservation
             assert free_after == free_before
         for k in ("cells_integrated", "cells_skipped", "cells_failed", "attempts", "accepted", "jacobians",
                   "lu_decompositions", "rhs_evaluations", "linear_solves"):
