@@ -165,6 +165,15 @@ extern "C" fcs_status fcs_set_options(fcs_ctx* ctx, const fcs_options* o) {
     return FCS_OK;
 }
 
+extern "C" fcs_status fcs_formation_enthalpy(fcs_ctx* ctx, double* hf) {
+    if (!ctx || !hf) return FCS_ERR_INVALID;
+    if (!ctx->loaded) return set_err(ctx, FCS_ERR_STATE, "no mechanism loaded");
+    if (fcs_status s = refuse_if_async_pending(ctx)) return s;
+    cudaSetDevice(ctx->device);
+    CK(cudaMemcpy(hf, ctx->M.hf, ctx->M.ns * sizeof(double), cudaMemcpyDeviceToHost));
+    return FCS_OK;
+}
+
 extern "C" fcs_status fcs_mechanism_size(const fcs_ctx* ctx, int32_t* ns, int32_t* nr) {
     if (!ctx || !ctx->loaded) return FCS_ERR_STATE;
     if (ns) *ns = ctx->M.ns;

@@ -491,6 +491,7 @@ extern "C" fcs_status fcs_read_chemistry_properties(const char* path, fcs_option
         }
         if (as_word(gd->find("mapping"), w)) {
             if (w == "auto") o->mapping = FCS_MAPPING_AUTO;
+            else if (w == "lane") o->mapping = FCS_MAPPING_LANE;
             else if (w == "warp") o->mapping = FCS_MAPPING_WARP;
             else if (w == "block64") o->mapping = FCS_MAPPING_BLOCK64;
             else if (w == "block128") o->mapping = FCS_MAPPING_BLOCK128;

@@ -32,7 +32,7 @@ EXPORTS = ("fcs_create", "fcs_destroy", "fcs_last_error_string", "fcs_version", 
            "fcs_default_options",
            "fcs_set_options", "fcs_mechanism_size", "fcs_integrate", "fcs_integrate_lts",
            "fcs_integrate_noalloc", "fcs_integrate_async", "fcs_sync", "fcs_sync_timeout",
-           "fcs_test_fail_allocations", "fcs_rhs", "fcs_tc",
+           "fcs_test_fail_allocations", "fcs_formation_enthalpy", "fcs_rhs", "fcs_tc",
            "fcs_jacobian", "fcs_rates", "fcs_bench_fp64_peak", "fcs_bench_fp32_peak", "fcs_check_exp",
            # include/fcs_mlp.h
            "fcs_mlp_create", "fcs_mlp_destroy", "fcs_mlp_last_error", "fcs_mlp_get_shape", "fcs_mlp_param_count",
@@ -123,6 +123,7 @@ def load(path: str = LIB) -> C.CDLL:
     L.fcs_default_options.argtypes = [C.POINTER(Options)]
     L.fcs_set_options.argtypes = [vp, C.POINTER(Options)]
     L.fcs_mechanism_size.argtypes = [vp, _ip, _ip]
+    L.fcs_formation_enthalpy.argtypes = [vp, _dp]
     cell_args = [vp, C.c_int64, C.c_double, vp, vp, vp, vp, vp, vp, vp, C.POINTER(StepStats), _dp, C.c_int32]
     L.fcs_integrate.argtypes = cell_args
     L.fcs_integrate_lts.argtypes = [vp, C.c_int64, vp] + cell_args[3:]

@@ -90,5 +90,40 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
     return LIB
 
 
+PLUGIN = os.path.join(PKG, "plugin")
+PLUGIN_BUILD = os.path.join(PLUGIN, "_build")
+PLUGIN_LIB = os.path.join(PLUGIN_BUILD, "libFastChemistryModel.so")
+STUB_LIB = os.path.join(PLUGIN_BUILD, "libfoamStub.so")
+
+
+def build_plugin(verbose: bool = False) -> str:
+    """libFastChemistryModel.so, the OpenFOAM-side plugin (plugin/), built
+    against the OpenFOAM-10 stub of plugin/foam_stub (libfoamStub.so, which
+    holds the chemistry-solver selection table) and libfcs_cuda.so.  With an
+    OpenFOAM-10 installation the same sources are built by wmake (plugin/Make)."""
+    lib = build(verbose=verbose)
+    os.makedirs(PLUGIN_BUILD, exist_ok=True)
+    inc = ["-I" + PLUGIN, "-I" + os.path.join(PLUGIN, "foam_stub"), "-I" + os.path.join(os.path.dirname(PKG), "include")]
+    stub_src = os.path.join(PLUGIN, "foam_stub", "foamStub.C")
+    srcs = [os.path.join(PLUGIN, f) for f in os.listdir(PLUGIN) if f.endswith((".C", ".H"))]
+    srcs += [os.path.join(PLUGIN, "foam_stub", f) for f in os.listdir(os.path.join(PLUGIN, "foam_stub"))]
+    cmds = []
+    if _stale(STUB_LIB, [stub_src] + srcs):
+        cmds.append(["g++"] + CXXFLAGS + inc + ["-shared", stub_src, "-o", STUB_LIB])
+    if _stale(PLUGIN_LIB, srcs + [lib, os.path.join(os.path.dirname(PKG), "include", "fcs.h")]):
+        cmds.append(["g++"] + CXXFLAGS + inc + ["-shared", os.path.join(PLUGIN, "odeChemistrySolvers.C"),
+                                                "-o", PLUGIN_LIB, "-L" + LIBDIR, "-lfcs_cuda",
+                                                "-L" + PLUGIN_BUILD, "-lfoamStub",
+                                                "-Wl,-rpath," + LIBDIR, "-Wl,-rpath," + PLUGIN_BUILD])
+    for cmd in cmds:
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if verbose or r.returncode != 0:
+            sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+        if r.returncode != 0:
+            raise RuntimeError("plugin build failed")
+    return PLUGIN_LIB
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv, force="-f" in sys.argv))
+    print(build_plugin(verbose="-v" in sys.argv))

@@ -232,6 +232,11 @@ fcs_status fcs_set_options(fcs_ctx* ctx, const fcs_options* opts);
 /* Number of species / reactions of the loaded mechanism. */
 fcs_status fcs_mechanism_size(const fcs_ctx* ctx, int32_t* n_species, int32_t* n_reactions);
 
+/* hf[Ns]: each species' formation enthalpy at 298.15 K in J/kg, as
+ * specieThermo::Hf() gives it; the chemistry model's Qdot() is
+ * -sum_i hf_i RR_i over the last solve's RR (FastChemistryModel.C:656-685). */
+fcs_status fcs_formation_enthalpy(fcs_ctx* ctx, double* hf);
+
 /*
  * Integrate n_cells independent constant-pressure cells over delta_t.
  * Batched form of FastChemistryModel::solve(deltaT) (transientSolve.H:30-104):
