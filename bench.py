@@ -179,8 +179,11 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-PORT_NOTE = ("oracle port (scalar C restatement): the reference core needs x86 AVX2 and glibc libmvec and "
-             "does not build on this host; per core it is slower than the reference's vectorised core")
+PORT_NOTE = ("oracle port (scalar C restatement): the reference core's sources are not present on this host; "
+             "per core the port is slower than the reference's vectorised core")
+REF_NOTE = ("the reference's own numerical core (Reaction/, LUsolver/, ODE/Opt*) compiled unmodified: with AVX2/FMA "
+            "and libmvec on x86-64; on other hosts with the portable SIMD shim (oracle/simd_shim: the AVX "
+            "intrinsics on GCC vector extensions, libmvec's exp/log/pow as scalar libm)")
 
 
 def cpu_integrator(flat, w):
@@ -195,50 +198,69 @@ def cpu_integrator(flat, w):
                                                 treact=w.treact, threads=threads)), "port"
 
 
-def cpu_baseline(flat, w, cells, seconds, threads, stats=None):
+class CellSampler:
+    """Disjoint randomly chosen cells of the field, in one seeded order that
+    continues across calls (wrapping around after the whole field), so that
+    successive CPU steps integrate fresh cells."""
+
+    def __init__(self, n, seed=7):
+        self.order = np.random.default_rng(seed).permutation(n)
+        self.pos = 0
+
+    def take(self, k):
+        n = self.order.size
+        idx = self.order[np.arange(self.pos, self.pos + k) % n]
+        self.pos += k
+        return idx
+
+
+def cpu_baseline(flat, w, cells, seconds, threads, sampler, stats=None):
     """The reference CPU integrator (its own core, else the oracle port) on a
-    bounded sample of the workload's cells (all host threads).  Returns
+    bounded sample of the workload's cells (all host threads): batches of
+    fresh cells from `sampler` until about `seconds` of wall time.  Returns
     (cells/s, cells done, seconds, kind); `stats` (a dict) also gets the
     attempts per cell (Jacobians per cell: one per Rosenbrock attempt)."""
     run, kind = cpu_integrator(flat, w)
-    rng = np.random.default_rng(7)
-    order = rng.permutation(cells.n)
     n = max(threads * 2, 32)
     t_used = 0.0
     done = 0
     jac = 0
     while True:
-        sub = cells.subset(order[done:done + n])
+        sub = cells.subset(sampler.take(n))
         t0 = time.perf_counter()
         out = run(sub, threads)
         dt = time.perf_counter() - t0
         jac += int(out["counters"]["jacobians"])
         t_used += dt
         done += sub.n
-        if t_used >= seconds or done >= cells.n:
+        if t_used >= seconds:
             break
         rate = done / t_used
-        n = int(min(cells.n - done, max(threads, rate * (seconds - t_used))))
-        if n <= 0:
-            break
+        n = int(max(threads, rate * (seconds - t_used)))
     if stats is not None:
         stats["jacobians_per_cell"] = jac / max(1, done)
     return done / t_used, done, t_used, kind
 
 
-def cpu_single_core(flat, w, cells, seconds):
-    """One host thread on a few cells of the same sample order: cells/s."""
+def cpu_single_core(flat, w, cells, seconds, sampler):
+    """One host thread on a few fresh cells: cells/s."""
     run, _ = cpu_integrator(flat, w)
-    order = np.random.default_rng(7).permutation(cells.n)
     done, t_used, n = 0, 0.0, 2
-    while t_used < seconds and done < cells.n:
-        sub = cells.subset(order[done:done + n])
+    while t_used < seconds:
+        sub = cells.subset(sampler.take(n))
         t0 = time.perf_counter()
         run(sub, 1)
         t_used += time.perf_counter() - t0
         done += sub.n
-        n = max(1, min(cells.n - done, int(done / t_used * max(0.5, seconds - t_used)) + 1))
+        n = max(1, int(done / t_used * max(0.5, seconds - t_used)) + 1)
     return done / t_used
+
+
+def workload_config(w, mech, n, solver, precision):
+    """The `config` object both arms print: the workload and how it is solved."""
+    return {"workload": w.name, "cells": n, "species": mech.n_species, "reactions": mech.n_reactions,
+            "solver": solver, "precision": precision, "jacobian": w.jacobian, "dt": w.dt,
+            "abs_tol": w.abs_tol, "rel_tol": w.rel_tol, "initial_sub_dt": w.sub_dt0, "treact": w.treact}
 
 
 def reference_arm(args):
@@ -246,35 +268,38 @@ def reference_arm(args):
     if rank != 0:
         return
     import fcs
-    w = fcs.WORKLOADS[args.workload]
+    w = workload(args)
     mech = w.mechanism()
     flat = fcs.flatten(mech)
     import oracle
-    oracle.build(ref=True)  # the reference core only where its sources are present (x86-64)
+    oracle.build(ref=True)  # the reference core where it builds (AVX2 on x86-64, the SIMD shim elsewhere)
     cells = fcs.cells_for(w, mech, n=args.cells or None)
     threads = os.cpu_count() or 1
     per_step = max(2.0, args.cpu_seconds / max(1, args.steps))
+    sampler = CellSampler(cells.n)
     for _ in range(max(0, min(args.warmup, 1))):
-        cpu_baseline(flat, w, cells.subset(np.arange(min(cells.n, threads))), 0.1, threads)
-    rates, total, kind, extra = [], 0, "port", {}
+        cpu_baseline(flat, w, cells, 0.1, threads, CellSampler(cells.n, seed=8))
+    rates, secs, total, kind, extra = [], [], 0, "port", {}
     for _ in range(args.steps):
-        r, n, _t, kind = cpu_baseline(flat, w, cells, per_step, threads, extra)
+        r, n, t, kind = cpu_baseline(flat, w, cells, per_step, threads, sampler, extra)
         rates.append(r)
+        secs.append(t)
         total += n
-    value = statistics.median(rates)
-    sample = f"{total} cells of {cells.n} over {args.steps} steps, each step ~{per_step:.0f} s of CPU work"
+    value = total / sum(secs)
+    sample = (f"{total} distinct cells of the {cells.n}-cell field (seeded random order) over {args.steps} steps "
+              f"of ~{per_step:.0f} s each, {total / max(1, args.steps):.0f} cells per step; ms_per_step is the "
+              f"measured wall time of a step's sample")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": cells.n / value * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(secs),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)",
-            "config": {"workload": w.name, "cells": cells.n, "solver": w.solver, "precision": "fp64",
-                       "dt": w.dt, "abs_tol": w.abs_tol, "rel_tol": w.rel_tol},
+            "data": "synthetic (seeded generator, no dataset)",
+            "config": workload_config(w, mech, cells.n, w.solver, "fp64"),
             "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": kind,
                              "sample": sample, "jacobians_per_cell": extra.get("jacobians_per_cell"),
-                             "single_core": cpu_single_core(flat, w, cells, min(5.0, per_step / 2))},
+                             "step_rates": rates,
+                             "single_core": cpu_single_core(flat, w, cells, min(5.0, per_step / 2), sampler)},
             "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    if kind == "port":
-        line["cpu_baseline"]["note"] = PORT_NOTE
+    line["cpu_baseline"]["note"] = PORT_NOTE if kind == "port" else REF_NOTE
     print(json.dumps(line), flush=True)
 
 
@@ -309,6 +334,34 @@ def accuracy(ctx, w, cells, idx, results, dev):
                      "p99_rel_T": float(np.percentile(eT[act], 99)) if act.any() else 0.0,
                      "max_abs_Y": float(eY[act].max()) if act.any() else 0.0}
     return out
+
+
+def accuracy_cpu(flat, w, cells, idx, results):
+    """Max / p99 relative T and max absolute Y error of each result on cells
+    `idx` against the reference's CPU Rodas34 (its own core where it is built,
+    else the oracle port) at absTol 1e-14 / relTol 1e-10."""
+    import oracle
+    sub = cells.subset(idx)
+    threads = os.cpu_count() or 1
+    if os.path.exists(oracle.REF_SO):
+        ref = oracle.Reference(flat, solver="OptRodas34", abs_tol=1e-14, rel_tol=1e-10, max_steps=10 ** 7)
+        out = ref.integrate(sub, w.dt, treact=w.treact, threads=threads)
+        name = "the reference's own CPU core"
+    else:
+        out = oracle.Port(flat).integrate(sub, w.dt, solver="OptRodas34", abs_tol=1e-14, rel_tol=1e-10,
+                                          max_steps=10 ** 7, treact=w.treact, threads=threads)
+        name = "the oracle port of the reference's CPU integrator"
+    Tt, Yt = out["T"], out["Y"]
+    act = sub.T > w.treact
+    res = {"reference": f"{name}, OptRodas34 at absTol 1e-14, relTol 1e-10, maxSteps 1e7 on the sampled cells",
+           "cells": int(idx.size)}
+    for name_r, (T, Y) in results.items():
+        eT = np.abs(T[idx] - Tt) / Tt
+        eY = np.abs(Y[:, idx] - Yt).max(axis=0)
+        res[name_r] = {"max_rel_T": float(eT[act].max()) if act.any() else 0.0,
+                       "p99_rel_T": float(np.percentile(eT[act], 99)) if act.any() else 0.0,
+                       "max_abs_Y": float(eY[act].max()) if act.any() else 0.0}
+    return res
 
 
 def args_solver(o):
@@ -492,9 +545,14 @@ def main():
     if args.accuracy_cells > 0:
         rng = np.random.default_rng(5)
         idx = np.sort(rng.choice(n, min(n, args.accuracy_cells), replace=False))
-        acc = accuracy(ctx, w, cells, idx, results, dev)
-        acc["reference"] = "GPU FP64 integrator at absTol 1e-14, relTol 1e-10, maxSteps 1e7 on the sampled cells"
-        acc["cells"] = int(idx.size)
+        gpu_tight = accuracy(ctx, w, cells, idx, results, dev)
+        gpu_tight["reference"] = "GPU FP64 integrator at absTol 1e-14, relTol 1e-10, maxSteps 1e7 on the sampled cells"
+        gpu_tight["cells"] = int(idx.size)
+        # the FP64 oracle proper: the reference's CPU integrator at the tight
+        # tolerances on the first cells of the same sample
+        cidx = idx[:min(idx.size, 32)]
+        acc = accuracy_cpu(flat, w, cells, cidx, results)
+        acc["gpu_tight"] = gpu_tight
     # roofline of the integrator kernel
     f64, f32, n_exp = flops_per_attempt(ns, mech.n_reactions, mech.count(1), mech.count(2), args.solver,
                                         args.precision)
@@ -515,12 +573,11 @@ def main():
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32",
             "data": "synthetic (seeded generator, no dataset)",
-            "config": {"workload": w.name, "cells": n, "species": ns, "reactions": mech.n_reactions,
-                       "solver": args.solver, "precision": args.precision, "jacobian": w.jacobian,
-                       "dt": w.dt, "abs_tol": w.abs_tol, "rel_tol": w.rel_tol, "method": "plain GPU " + args.solver,
-                       "step": "one CUDA graph per step (classify, binned work queue, persistent integrator)",
-                       "l2": "flushed (256 MB write) before every timed step",
-                       "parallelism": f"replicas x{ws} (cells independent, no collective)"},
+            "config": workload_config(w, mech, n, args.solver, args.precision),
+            "setup": {"method": "plain GPU " + args.solver, "mapping": s0["mapping"],
+                      "step": "one CUDA graph per step (classify, binned work queue, persistent integrator)",
+                      "l2": "flushed (256 MB write) before every timed step",
+                      "parallelism": f"replicas x{ws} (cells independent, no collective)"},
             "e2e": {"value": ws * n / (t_e2e * 1e-3), "unit": "cells/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": 3 * args.steps,  # classify_bin_kernel, queue_kernel, integrate_kernel
@@ -539,13 +596,14 @@ def main():
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         extra = {}
-        rate, done, tu, kind = cpu_baseline(flat, w, cells, args.cpu_seconds, threads, extra)
+        sampler = CellSampler(cells.n)
+        rate, done, tu, kind = cpu_baseline(flat, w, cells, args.cpu_seconds, threads, sampler, extra)
         line["cpu_baseline"] = {"value": rate, "unit": "cells/s", "cores": threads, "kind": kind,
-                                "sample": f"{done} randomly chosen cells of the same field, {tu:.1f} s of CPU time",
+                                "sample": f"{done} distinct cells of the same field (seeded random order), "
+                                          f"{tu:.1f} s of wall time",
                                 "jacobians_per_cell": extra["jacobians_per_cell"],
-                                "single_core": cpu_single_core(flat, w, cells, min(5.0, args.cpu_seconds / 3))}
-        if kind == "port":
-            line["cpu_baseline"]["note"] = PORT_NOTE
+                                "single_core": cpu_single_core(flat, w, cells, min(5.0, args.cpu_seconds / 3), sampler),
+                                "note": PORT_NOTE if kind == "port" else REF_NOTE}
     print(json.dumps(line), flush=True)
 
 

@@ -81,5 +81,9 @@ def test_reference_arm_line(monkeypatch, capsys):
     cb = line["cpu_baseline"]
     assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["value"] == line["value"]
     assert cb["jacobians_per_cell"] > 1 and cb["single_core"] > 0
-    assert (cb["kind"] == "port") == ("note" in cb)
+    assert "note" in cb and cb["note"].startswith("oracle port") == (cb["kind"] == "port")
     assert line["config"]["workload"] == "counterflow_53s"
+    # the same config keys as the GPU arm's line, and a measured step time
+    for k in ("cells", "species", "reactions", "solver", "precision", "jacobian", "dt", "abs_tol", "rel_tol"):
+        assert k in line["config"], k
+    assert 0 < line["ms_per_step"] < 60e3
