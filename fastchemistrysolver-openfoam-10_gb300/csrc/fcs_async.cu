@@ -59,6 +59,10 @@ extern "C" fcs_status fcs_integrate_async(fcs_ctx* ctx, int64_t nc, double dt, c
     io.p = p; io.rho0 = rho0; io.T = T; io.Y = Y; io.subDt = sub; io.RR = RR; io.status = status;
     io.stats = ctx->bStats.p;
     io.dtMinBits = ctx->bMin.p;
+    if (ctx->bAtt.n < (size_t)std::max<int64_t>(nc, 1)) ctx->attN = 0;
+    CK(ctx->bAtt.ensure(std::max<int64_t>(nc, 1)));
+    io.attempts = ctx->bAtt.p;
+    io.attemptsValid = (sorted && ctx->attN == nc) ? 1 : 0;
     CK(cudaEventRecord(ctx->evc0, st));
     CK(cudaMemsetAsync(ctx->bStats.p, 0, ST_COUNT * sizeof(long long), st));
     CK(cudaMemsetAsync(ctx->bMin.p, 0x7f, sizeof(unsigned long long), st));
@@ -78,6 +82,7 @@ extern "C" fcs_status fcs_integrate_async(fcs_ctx* ctx, int64_t nc, double dt, c
     CK(cudaEventRecord(ctx->evc1, st));
     CK(cudaEventRecord(ctx->evAsync, st));
     ctx->asyncPending = true;
+    ctx->attN = nc;
     ctx->asyncDt = dt;
     ctx->asyncGroup = group;
     return FCS_OK;

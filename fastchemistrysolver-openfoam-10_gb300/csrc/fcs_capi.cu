@@ -134,7 +134,7 @@ extern "C" fcs_status fcs_destroy(fcs_ctx* ctx) {
     ctx->dRx.release();
     ctx->dPlogOff.release(); ctx->dIncOff.release(); ctx->dInc.release(); ctx->dTbInc.release();
     ctx->bStatus.release(); ctx->bOrder.release(); ctx->bHead.release();
-    ctx->bStats.release(); ctx->bMin.release(); ctx->gws.release(); ctx->bBin.release();
+    ctx->bStats.release(); ctx->bMin.release(); ctx->gws.release(); ctx->bBin.release(); ctx->bAtt.release();
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     if (ctx->hStats) cudaFreeHost(ctx->hStats);
     if (ctx->evAsync) cudaEventDestroy(ctx->evAsync);
@@ -412,7 +412,7 @@ static bool make_lane_shape(fcs_ctx* ctx, bool integrate, Shape& sh) {
     sh.lc.block = kBlock;
     sh.lc.grid = ctx->numSMs * perSM;
     sh.L = SlotLayout{};
-    sh.L.bytes = make_lane_layout(ctx->M.ns, ctx->M.nTB, mixed).words * (int)sizeof(double);
+    sh.L.bytes = make_lane_layout(ctx->M.ns, ctx->M.nr, ctx->M.nTB, mixed).words * (int)sizeof(double);
     return true;
 }
 
@@ -599,6 +599,12 @@ static fcs_status integrate_impl(fcs_ctx* ctx, int64_t nc, double dt, const doub
     if (sorted) CK(ctx->bBin.ensure(std::max<int64_t>(nc, 1)));
     io.stats = ctx->bStats.p;
     io.dtMinBits = ctx->bMin.p;
+    // per-cell attempts of the previous call on a batch of this size order the
+    // queue (the cells' costs change slowly from one CFD step to the next)
+    if (ctx->bAtt.n < (size_t)std::max<int64_t>(nc, 1)) ctx->attN = 0;
+    CK(ctx->bAtt.ensure(std::max<int64_t>(nc, 1)));
+    io.attempts = ctx->bAtt.p;
+    io.attemptsValid = (sorted && ctx->attN == nc) ? 1 : 0;
     const KOpts ko = kopts(ctx->opt);
     // The step's device work: counters, classify (cells with T <= Treact are
     // skipped, transientSolve.H:39, 70-76), the queue ordered by predicted
@@ -642,6 +648,8 @@ static fcs_status integrate_impl(fcs_ctx* ctx, int64_t nc, double dt, const doub
         key.internal[0] = ctx->bStats.p; key.internal[1] = ctx->bMin.p; key.internal[2] = ctx->bHead.p;
         key.internal[3] = ctx->bOrder.p; key.internal[4] = ctx->bBin.p; key.internal[5] = ctx->gws.p;
         key.internal[6] = ctx->hStats;
+        key.internal[7] = ctx->bAtt.p;
+        key.attValid = io.attemptsValid;
         key.mech = ctx->M.rx;
         if (!ctx->gexec || std::memcmp(&key, &ctx->gkey, sizeof(key)) != 0) {
             if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
@@ -689,6 +697,7 @@ static fcs_status integrate_impl(fcs_ctx* ctx, int64_t nc, double dt, const doub
         CK(cudaMemcpyAsync(hs, ctx->bStats.p, ST_COUNT * sizeof(long long), cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(hmin, ctx->bMin.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     }
+    ctx->attN = nc;  // this call's kernels record the attempts of its cells
     if (!dev) {
         CK(cudaMemcpyAsync(T, io.T, nc * 8, cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(Y, io.Y, (size_t)ns * nc * 8, cudaMemcpyDeviceToHost, st));

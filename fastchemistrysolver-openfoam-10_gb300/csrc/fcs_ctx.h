@@ -52,6 +52,7 @@ struct GraphKey {
     fcs_options opt;
     int group;
     int sorted;
+    int attValid;             // the queue is ordered by the previous call's per-cell attempts
 };
 
 struct GateState;             // surrogate gate (fcs_gate.cu)
@@ -89,6 +90,9 @@ struct fcs_ctx {
     fcs::DBuf<char> gws;
     std::map<std::tuple<int, int, int, int>, int> tuned;  // (n, precision, solver, jac) -> group
     fcs::GateState* gate = nullptr;                       // attached surrogate, if any
+    // per-cell attempts of the last integration, for the cost-ordered queue
+    fcs::DBuf<int> bAtt;
+    long long attN = 0;                                   // batch size bAtt describes (0: none)
     // CUDA-graph step (FCS_CUDA_GRAPH)
     fcs::DBuf<int> bBin;                                  // predicted-step bin per cell
     cudaGraphExec_t gexec = nullptr;

@@ -194,7 +194,7 @@ __host__ __device__ inline SlotLayout make_layout(int ns, int nr, int nTB, bool 
     L.offScale = o; if (mixed) o = align16(o + 2 * n * 8);
     L.offPiv = o;   o = align16(o + n * 4);
     L.rc = rc < 1 ? 1 : (nr > 0 && rc > nr ? nr : rc);
-    L.offRx = o;    o = align16(o + 4 * L.rc * 8);
+    L.offRx = o;    o = align16(o + (4 * L.rc * 8 > n * 4 ? 4 * L.rc * 8 : n * 4));  // also the LU's permutation scratch
     L.offCur = o;   o = align16(o + ns * 4);
     L.offTb = o;    o = align16(o + 2 * (nTB > 0 ? nTB : 1) * 8);
     L.offTable = o;
@@ -1170,8 +1170,10 @@ __device__ __forceinline__ int choose_pivot(const MT* A, int ld, int k, int pos,
     return (fabs(double(A[(size_t)k * ld + k])) < fabs(double(A[(size_t)(k + 1) * ld + k]))) ? k + 1 : k;
 }
 
+// work: n ints of slot scratch that is free during the factorisation (the
+// permutation is built there and copied over piv).
 template<int G, class MT>
-__device__ __noinline__ void lu_factor(const Grp<G>& g, MT* A, int n, int ld, int* piv, double* invD) {
+__device__ __noinline__ void lu_factor(const Grp<G>& g, MT* A, int n, int ld, int* piv, double* invD, int* work) {
     const int rem = n & 3;
     constexpr int TC = 8, TR = G / TC;
     const int tr = g.rank / TC, tc = g.rank % TC;
@@ -1215,16 +1217,17 @@ __device__ __noinline__ void lu_factor(const Grp<G>& g, MT* A, int n, int ld, in
         g.sync();
     }
     // The interchange sequence as one gather permutation (P b)[i] = b[perm[i]]
-    // for the solves, written over piv.
+    // for the solves, built in the slot scratch and written over piv.
+    for (int i = g.rank; i < n; i += G) work[i] = i;
+    g.sync();
     if (g.rank == 0) {
-        int perm[256];
-        for (int i = 0; i < n; i++) perm[i] = i;
         for (int j = 0; j < n; j++) {
             const int pj = piv[j];
-            if (pj != j) { const int t = perm[j]; perm[j] = perm[pj]; perm[pj] = t; }
+            if (pj != j) { const int t = work[j]; work[j] = work[pj]; work[pj] = t; }
         }
-        for (int i = 0; i < n; i++) piv[i] = perm[i];
     }
+    g.sync();
+    for (int i = g.rank; i < n; i += G) piv[i] = work[i];
     g.sync();
 }
 

@@ -23,6 +23,12 @@ __global__ void classify_kernel(CellIO io, int ns, double Treact, int* order, in
 __device__ __forceinline__ int step_bin(double deltaT, double sub) {
     const double steps = deltaT / fmax(sub, 1e-300);
     int b = steps > 1 ? (int)log2(steps) : 0;
+    return b < 0 ? 0 : (b >= 32 ? 31 : b);
+}
+
+// eight bins per octave of the previous integration's attempts (8 .. 2048)
+__device__ __forceinline__ int attempt_bin(int attempts) {
+    const int b = (int)floorf(8.f * log2f((float)(attempts > 1 ? attempts : 1))) - 24;
     return b < 0 ? 0 : (b >= kQueueBins ? kQueueBins - 1 : b);
 }
 
@@ -35,7 +41,7 @@ __global__ void classify_bin_kernel(CellIO io, int ns, double Treact, int* bin, 
          c += (long long)gridDim.x * blockDim.x) {
         if (io.T[c] > Treact) {
             const double deltaT = io.dtPerCell ? io.dtPerCell[c] : io.deltaT;
-            const int b = step_bin(deltaT, io.subDt[c]);
+            const int b = io.attemptsValid ? attempt_bin(io.attempts[c]) : step_bin(deltaT, io.subDt[c]);
             bin[c] = b;
             atomicAdd(&hist[b], 1);
         } else {

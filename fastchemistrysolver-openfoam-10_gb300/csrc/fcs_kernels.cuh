@@ -141,7 +141,8 @@ template<int G, class MT>
 __device__ __forceinline__ void factor_iteration(const Grp<G>& g, const DevMech& M, const Slot<MT>& s, double c) {
     if constexpr (sizeof(MT) == 8) form_iteration_matrix<G>(g, s, M.n, c);
     else form_iteration_matrix_scaled<G>(g, s, M.n, c);
-    lu_factor<G, MT>(g, s.LU, M.n, s.ld, s.piv, s.invD);
+    // the reaction-chunk arrays are free between a Jacobian and the next RHS
+    lu_factor<G, MT>(g, s.LU, M.n, s.ld, s.piv, s.invD, reinterpret_cast<int*>(s.Kf));
 }
 
 template<int G, class MT>
@@ -841,6 +842,7 @@ integrate_kernel(const DevMech M, const KOpts o, const SlotLayout L, CellIO io, 
         g.sync();
         const double subDt0 = io.subDt[c];
         double subDt = subDt0;
+        const long long att0 = cc.attempts;
         int st = FCS_CELL_OK;
         double timeLeft = deltaT;
         while (timeLeft > kSmall) {
@@ -882,6 +884,7 @@ integrate_kernel(const DevMech M, const KOpts o, const SlotLayout L, CellIO io, 
             dtMin = fmin(dtMin, subDt);
             io.subDt[c] = subDt < o.dtChemMax ? subDt : o.dtChemMax;
             if (io.status) io.status[c] = st;
+            if (io.attempts) io.attempts[c] = (int)(cc.attempts - att0);
         }
         g.sync();
     }

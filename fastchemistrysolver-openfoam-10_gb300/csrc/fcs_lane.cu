@@ -6,7 +6,7 @@ namespace fcs {
 cudaError_t launch_lane_integrate(const LaunchCfg& lc, bool mixed, const DevMech& M, const KOpts& o,
                                   const CellIO& io, const WorkQueue& q, char* gws, cudaStream_t st) {
     if (mixed || !gws || lc.block % 32 != 0) return cudaErrorInvalidValue;
-    const LaneLayout L = make_lane_layout(M.ns, M.nTB, false);
+    const LaneLayout L = make_lane_layout(M.ns, M.nr, M.nTB, false);
     auto k = lane_integrate_kernel<double>;
     // the workspace lives in global memory: all of the unified L1/shared
     // memory as L1, which caches the lanes' vectors and species arrays

@@ -52,6 +52,7 @@ struct LaneSlot {
     LA<int> piv;
     LA<float> LU32, x32;   // mixed precision
     LA<double> dr, dc;     // mixed precision equilibration
+    LA<double> q, dq;      // per-reaction net rate and d/dT
     __device__ __forceinline__ LA<double> v(int k) const { return vec + k * n; }
 };
 
@@ -76,7 +77,40 @@ __device__ __forceinline__ LaneSlot make_lane_slot(double* ws, const LaneLayout&
     s.dr = LA<double>{base + (size_t)L.offScale * kLanes};
     s.dc = s.dr + L.n;
     s.x32 = LA<float>{reinterpret_cast<float*>(ws + (size_t)L.offX32 * kLanes) + lane};
+    s.q = LA<double>{base + (size_t)L.offRx * kLanes};
+    s.dq = s.q + (L.nr > 0 ? L.nr : 1);
     return s;
+}
+
+// A mechanism array indexed like a per-lane one (the same address in every
+// lane): lane_map inputs.
+struct LAC {
+    const double* p;
+    __device__ __forceinline__ double operator[](int e) const { return __ldg(p + e); }
+};
+// eff[e] * w
+struct LAE {
+    const double* p;
+    double w;
+    __device__ __forceinline__ double operator[](int e) const { return __ldg(p + e) * w; }
+};
+
+// Memory-level parallelism: a lane's array accesses go to L1/L2/HBM, so a
+// loop whose iterations each wait for their own load runs at the memory
+// latency.  The loops below issue the loads of several elements before they
+// use or store any of them (the compiler cannot move a load above an earlier
+// store to a per-lane array, which might alias).
+
+// out[i] = f(in[i]...) for i < n, four elements per step
+template<class F, class... In>
+__device__ __forceinline__ void lane_map(int n, LA<double> out, F f, In... in) {
+    int i = 0;
+    for (; i + 4 <= n; i += 4) {
+        double r0 = f(in[i]...), r1 = f(in[i + 1]...), r2 = f(in[i + 2]...), r3 = f(in[i + 3]...);
+        out[i] = r0; out[i + 1] = r1; out[i + 2] = r2; out[i + 3] = r3;
+    }
+    #pragma unroll 1
+    for (; i < n; i++) out[i] = f(in[i]...);
 }
 
 // ------------------------------------------------------------------------
@@ -95,6 +129,38 @@ __device__ __forceinline__ double lane_inv_kc(const RxnInfo& x, const LA<double>
     return v > cl ? cl : v;
 }
 
+// The species values of a reaction with at most 3 reactants and 3 products,
+// all loaded before any is used; products of 1..3 factors in the reference's
+// order (first factor, then the next ones).
+struct Tri { double a, b, c; };
+__device__ __forceinline__ Tri lane_load3(const LA<double>& X, const uint8_t* s) {
+    return Tri{X[s[0]], X[s[1]], X[s[2]]};  // unused slots hold species 0: a valid address
+}
+__device__ __forceinline__ double prod3(const Tri& t, int k) {
+    double v = t.a;
+    if (k > 1) v *= t.b;
+    if (k > 2) v *= t.c;
+    return v;
+}
+__device__ __forceinline__ double sum3(const Tri& t, int k) {
+    double v = t.a;
+    if (k > 1) v += t.b;
+    if (k > 2) v += t.c;
+    return v;
+}
+__device__ __forceinline__ bool short_reaction(const RxnInfo& x) { return x.nl <= 3 && x.nr <= 3; }
+
+// 1/Kc of a short reaction from preloaded E (reactants) and 1/E (products)
+__device__ __forceinline__ double inv_kc3(const RxnInfo& x, const Tri& e, const Tri& einv, const PFactor& pf) {
+    double v = prod3(e, x.nl);
+    v *= einv.a;
+    if (x.nr > 1) v *= einv.b;
+    if (x.nr > 2) v *= einv.c;
+    if (x.dnu != 0) v *= pressure_factor(pf, x.dnu);
+    const double cl = inv_kc_clamp(x);
+    return v > cl ? cl : v;
+}
+
 // Third-body concentrations M_t = sum_j eff[t][j] C_j (ThirdBodyFactor1D)
 __device__ __forceinline__ void lane_third_body(const DevMech& M, const LaneSlot& s) {
     const int ns = M.ns;
@@ -102,7 +168,7 @@ __device__ __forceinline__ void lane_third_body(const DevMech& M, const LaneSlot
     for (int t = 0; t < M.nTB; t++) {
         const double* e = M.eff + (size_t)t * ns;
         double m = 0;
-        #pragma unroll 4
+        #pragma unroll 8
         for (int j = 0; j < ns; j++) m = fma(__ldg(&e[j]), s.C[j], m);
         s.Mtb[t] = m;
     }
@@ -125,6 +191,29 @@ __device__ __forceinline__ double lane_kf(const DevMech& M, const RxnInfo& x, do
     return Kf;
 }
 
+// w_i = sum over the incidence list of species i (reaction order) of +-q[r],
+// four entries' loads at a time: the same order as the cell-group gather.
+__device__ __forceinline__ double lane_gather(const DevMech& M, const LA<double>& q, int i) {
+    const int e1 = __ldg(&M.incOff[i + 1]);
+    int e = __ldg(&M.incOff[i]);
+    double w = 0.0;
+    for (; e + 4 <= e1; e += 4) {
+        const int v0 = __ldg(&M.inc[e]), v1 = __ldg(&M.inc[e + 1]), v2 = __ldg(&M.inc[e + 2]), v3 = __ldg(&M.inc[e + 3]);
+        const double q0 = q[v0 >> 1], q1 = q[v1 >> 1], q2 = q[v2 >> 1], q3 = q[v3 >> 1];
+        w = (v0 & 1) ? w + q0 : w - q0;
+        w = (v1 & 1) ? w + q1 : w - q1;
+        w = (v2 & 1) ? w + q2 : w - q2;
+        w = (v3 & 1) ? w + q3 : w - q3;
+    }
+    #pragma unroll 1
+    for (; e < e1; e++) {
+        const int v = __ldg(&M.inc[e]);
+        const double qq = q[v >> 1];
+        w = (v & 1) ? w + qq : w - qq;
+    }
+    return w;
+}
+
 // RHS: FastChemistryModel::derivatives (FastChemistryModel.C:194-273 for mode
 // 1, 340-417 for mode 2) over OptReaction::dNdtByV (ReactionRate.C:732-1503).
 // YT is clamped (Y >= 0) in place; out[0..n) receives dY/dt and dT/dt.
@@ -135,29 +224,49 @@ __device__ __noinline__ void lane_rhs(const DevMech& M, const LaneSlot& s, doubl
     const double Tc = clampT(M, T);
     const double RuTByP = kRu * T / p;
     double part = 0;
-    #pragma unroll 1
-    for (int i = 0; i < ns; i++) {
-        const double y0 = YT[i];
-        const double y = y0 > 0 ? y0 : 0.0;
-        YT[i] = y;
-        part = fma(y * __ldg(&M.invW[i]), RuTByP, part);
+    {
+        int i = 0;
+        for (; i + 4 <= ns; i += 4) {
+            const double a0 = YT[i], a1 = YT[i + 1], a2 = YT[i + 2], a3 = YT[i + 3];
+            const double y0 = a0 > 0 ? a0 : 0.0, y1 = a1 > 0 ? a1 : 0.0, y2 = a2 > 0 ? a2 : 0.0,
+                         y3 = a3 > 0 ? a3 : 0.0;
+            YT[i] = y0; YT[i + 1] = y1; YT[i + 2] = y2; YT[i + 3] = y3;
+            part = fma(y0 * __ldg(&M.invW[i]), RuTByP, part);
+            part = fma(y1 * __ldg(&M.invW[i + 1]), RuTByP, part);
+            part = fma(y2 * __ldg(&M.invW[i + 2]), RuTByP, part);
+            part = fma(y3 * __ldg(&M.invW[i + 3]), RuTByP, part);
+        }
+        #pragma unroll 1
+        for (; i < ns; i++) {
+            const double y0 = YT[i];
+            const double y = y0 > 0 ? y0 : 0.0;
+            YT[i] = y;
+            part = fma(y * __ldg(&M.invW[i]), RuTByP, part);
+        }
     }
     const double invrhoM = part;
     const double rhoM = 1.0 / invrhoM;
     const double logT = log(Tc), invT = 1.0 / Tc;
     const double Tp = mode == 2 ? T : Tc;
     #pragma unroll 1
-    for (int i = 0; i < ns; i++) {
-        const double invW = __ldg(&M.invW[i]);
-        s.C[i] = rhoM * invW * YT[i];
-        const Nasa a = load_nasa(species_coeffs(M, i, Tc));
-        const double Ei = fast_exp(gibbs_exponent(a, Tc, invT, logT));
-        s.B[i] = Ei;
-        s.Binv[i] = 1.0 / Ei;
-        const double RuInvW = invW * kRu;
-        s.Cp[i] = cp_of(a, Tp, RuInvW);
-        s.Ha[i] = ha_of(a, Tp, RuInvW);
-        out[i] = 0.0;
+    for (int i = 0; i < ns; i += 2) {
+        // two species per step: both mass fractions loaded first
+        const int i1 = i + 1 < ns ? i + 1 : i;
+        const double ya = YT[i], yb = YT[i1];
+        #pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int k = u ? i1 : i;
+            if (u && i1 == i) break;
+            const double invW = __ldg(&M.invW[k]);
+            s.C[k] = rhoM * invW * (u ? yb : ya);
+            const Nasa a = load_nasa(species_coeffs(M, k, Tc));
+            const double Ei = fast_exp(gibbs_exponent(a, Tc, invT, logT));
+            s.B[k] = Ei;
+            s.Binv[k] = 1.0 / Ei;
+            const double RuInvW = invW * kRu;
+            s.Cp[k] = cp_of(a, Tp, RuInvW);
+            s.Ha[k] = ha_of(a, Tp, RuInvW);
+        }
     }
     lane_third_body(M, s);
     const PFactor pf = pressure_factors(Tc);
@@ -166,34 +275,52 @@ __device__ __noinline__ void lane_rhs(const DevMech& M, const LaneSlot& s, doubl
     #pragma unroll 1
     for (int r = 0; r < M.nr; r++) {
         const RxnInfo x = load_rx(M.rx + r);
-        double Kf, Kr = 0;
-        if (r >= sp0 && r < sp1) {
-            const SpecialK k = special_rates_m(M, x, x.tb >= 0 ? s.Mtb[x.tb] : 1.0, Tc, logT, invT, false);
-            Kf = k.Kf;
-            Kr = k.Kr;  // non-equilibrium: its own reverse rate
-            if (x.rev == 1) Kr = Kf * lane_inv_kc(x, s.B, s.Binv, pf);
+        const bool special = r >= sp0 && r < sp1;
+        double Kf, Kr = 0, CF, CR;
+        if (short_reaction(x)) {
+            const Tri cl = lane_load3(s.C, x.sl), cr = lane_load3(s.C, x.sr);
+            Tri el{0, 0, 0}, er{0, 0, 0};
+            const bool viaKc = special ? x.rev == 1 : x.rev != 0;
+            if (viaKc) { el = lane_load3(s.B, x.sl); er = lane_load3(s.Binv, x.sr); }
+            const double Mt = x.tb >= 0 ? s.Mtb[x.tb] : 1.0;
+            if (special) {
+                const SpecialK k = special_rates_m(M, x, Mt, Tc, logT, invT, false);
+                Kf = k.Kf;
+                Kr = k.Kr;  // non-equilibrium: its own reverse rate
+            } else {
+                double dk;
+                Kf = lane_kf(M, x, p, logP, logT, invT, &dk);
+                if (x.tb >= 0) Kf *= Mt;
+            }
+            if (viaKc) Kr = Kf * inv_kc3(x, el, er, pf);
+            CF = prod3(cl, x.nl);
+            CR = prod3(cr, x.nr);
         } else {
-            double dk;
-            Kf = lane_kf(M, x, p, logP, logT, invT, &dk);
-            if (x.tb >= 0) Kf *= s.Mtb[x.tb];
-            if (x.rev) Kr = Kf * lane_inv_kc(x, s.B, s.Binv, pf);
+            if (special) {
+                const SpecialK k = special_rates_m(M, x, x.tb >= 0 ? s.Mtb[x.tb] : 1.0, Tc, logT, invT, false);
+                Kf = k.Kf;
+                Kr = k.Kr;
+                if (x.rev == 1) Kr = Kf * lane_inv_kc(x, s.B, s.Binv, pf);
+            } else {
+                double dk;
+                Kf = lane_kf(M, x, p, logP, logT, invT, &dk);
+                if (x.tb >= 0) Kf *= s.Mtb[x.tb];
+                if (x.rev) Kr = Kf * lane_inv_kc(x, s.B, s.Binv, pf);
+            }
+            CF = s.C[x.sl[0]];
+            #pragma unroll 1
+            for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
+            CR = s.C[x.sr[0]];
+            #pragma unroll 1
+            for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
         }
-        double CF = s.C[x.sl[0]];
-        #pragma unroll 1
-        for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
-        double CR = s.C[x.sr[0]];
-        #pragma unroll 1
-        for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
-        const double qr = Kf * CF - Kr * CR;
-        #pragma unroll 1
-        for (int q = 0; q < x.nl; q++) { double& w = out[x.sl[q]]; w = w - qr; }
-        #pragma unroll 1
-        for (int q = 0; q < x.nr; q++) { double& w = out[x.sr[q]]; w = w + qr; }
+        s.q[r] = Kf * CF - Kr * CR;
     }
     double cpm = 0, dtd = 0;
     #pragma unroll 1
     for (int i = 0; i < ns; i++) {
-        const double dY = (__ldg(&M.W[i]) * invrhoM) * out[i];
+        const double w = lane_gather(M, s.q, i);
+        const double dY = (__ldg(&M.W[i]) * invrhoM) * w;
         out[i] = dY;
         cpm = fma(YT[i], s.Cp[i], cpm);
         dtd = fma(s.Ha[i], dY, dtd);
@@ -201,24 +328,60 @@ __device__ __noinline__ void lane_rhs(const DevMech& M, const LaneSlot& s, doubl
     out[ns] = -dtd / cpm;
 }
 
+// J[rows of the reaction][j] -/+= d: reactant rows minus, product rows plus,
+// in the reference's order (reactants then products).  dup: a species occurs
+// more than once among the reaction's rows (then the updates of one element
+// must follow each other); otherwise every row is loaded before any is stored.
+__device__ __forceinline__ void lane_scatter_column(const RxnInfo& x, LA<double> J, int n, int j, double d,
+                                                    bool dup) {
+    if (!dup && x.nl <= 3 && x.nr <= 3) {
+        double& a0 = J[x.sl[0] * n + j];
+        double& a1 = J[x.sl[1] * n + j];
+        double& a2 = J[x.sl[2] * n + j];
+        double& b0 = J[x.sr[0] * n + j];
+        double& b1 = J[x.sr[1] * n + j];
+        double& b2 = J[x.sr[2] * n + j];
+        const double va0 = a0, va1 = a1, va2 = a2, vb0 = b0, vb1 = b1, vb2 = b2;
+        a0 = va0 - d;
+        if (x.nl > 1) a1 = va1 - d;
+        if (x.nl > 2) a2 = va2 - d;
+        b0 = vb0 + d;
+        if (x.nr > 1) b1 = vb1 + d;
+        if (x.nr > 2) b2 = vb2 + d;
+        return;
+    }
+    #pragma unroll 1
+    for (int q = 0; q < x.nl; q++) { double& c = J[x.sl[q] * n + j]; c = c - d; }
+    #pragma unroll 1
+    for (int q = 0; q < x.nr; q++) { double& c = J[x.sr[q] * n + j]; c = c + d; }
+}
+
+__device__ __forceinline__ bool repeated_species(const RxnInfo& x) {
+    // participants are warp-uniform: integer compares on the reaction record
+    const int m = x.nl + x.nr;
+    for (int a = 0; a < m; a++) {
+        const int sa = a < x.nl ? x.sl[a] : x.sr[a - x.nl];
+        for (int b = a + 1; b < m; b++) {
+            const int sb = b < x.nl ? x.sl[b] : x.sr[b - x.nl];
+            if (sa == sb) return true;
+        }
+    }
+    return false;
+}
+
 // Analytic Jacobian (FastChemistryModel::jacobian, FastChemistryModel.C:489-572,
 // over ddNdtByVdcTp, Jacobian.C:5-1004, and the dC/dY conversion,
 // Jacobian.C:2814-2858 exact / 4541-4568 fast, 3709-3793 T column and row)
-// into J (row-major n x n), f = dy/dt; YT clamped in place.  tcAcc: a free
-// n-vector for the temperature-column sums.
+// into J (row-major n x n), f = dy/dt; YT clamped in place.
 __device__ __noinline__ void lane_jac(const DevMech& M, const LaneSlot& s, double p, LA<double> YT, LA<double> f,
-                                      LA<double> J, LA<double> tcAcc, int fast) {
+                                      LA<double> J, int fast) {
     const int ns = M.ns, n = M.n;
-    #pragma unroll 1
-    for (int i = 0; i < ns; i++) {
-        const double y0 = YT[i];
-        YT[i] = y0 > 0 ? y0 : 0.0;
-    }
+    lane_map(ns, YT, [](double y0) { return y0 > 0 ? y0 : 0.0; }, YT);
     const double T = YT[ns];
     const double Tc = clampT(M, T);
     const double RuTByP = (kRu * Tc) / p;
     double rs = 0, mws = 0;
-    #pragma unroll 1
+    #pragma unroll 4
     for (int i = 0; i < ns; i++) {
         const double y = YT[i], invW = __ldg(&M.invW[i]);
         rs = fma(RuTByP, y * invW, rs);
@@ -244,106 +407,125 @@ __device__ __noinline__ void lane_jac(const DevMech& M, const LaneSlot& s, doubl
         s.Ha[i] = ha_of(a, Tc, RuInvW);
         cpm = fma(y, cp, cpm);
         dcpm = fma(y, dcp, dcpm);
-        f[i] = 0.0;
-        tcAcc[i] = 0.0;
     }
     const double CpM = cpm, dCpMdT = dcpm;
     lane_third_body(M, s);
-    #pragma unroll 1
-    for (int idx = 0; idx < ns * n; idx++) J[idx] = 0.0;
+    {
+        int idx = 0;
+        const int m = ns * n;
+        for (; idx + 4 <= m; idx += 4) { J[idx] = 0.0; J[idx + 1] = 0.0; J[idx + 2] = 0.0; J[idx + 3] = 0.0; }
+        for (; idx < m; idx++) J[idx] = 0.0;
+    }
     const PFactor pf = pressure_factors(Tc);
     const double logP = M.nPlog ? log(p) : 0.0;
     const int sp0 = M.spBegin, sp1 = M.spBegin + M.nSp;
     #pragma unroll 1
     for (int r = 0; r < M.nr; r++) {
         const RxnInfo x = load_rx(M.rx + r);
+        const bool special = r >= sp0 && r < sp1;
+        const bool shortr = short_reaction(x);
         double Kf, dKfdT, dKfdC = 0, Kr = 0, dKrdT = 0, dKrdC = 0;
-        bool viaKc = false;
-        if (r >= sp0 && r < sp1) {
-            const SpecialK k = special_rates_m(M, x, x.tb >= 0 ? s.Mtb[x.tb] : 1.0, Tc, logT, invT, true);
+        const bool viaKc = special ? x.rev == 1 : x.rev != 0;
+        Tri cl{0, 0, 0}, cr{0, 0, 0};
+        double Mt = 1.0;
+        if (shortr) {
+            cl = lane_load3(s.C, x.sl);
+            cr = lane_load3(s.C, x.sr);
+        }
+        if (x.tb >= 0) Mt = s.Mtb[x.tb];
+        if (special) {
+            const SpecialK k = special_rates_m(M, x, Mt, Tc, logT, invT, true);
             Kf = k.Kf; dKfdT = k.dKfdT; dKfdC = k.dKfdC;
             Kr = k.Kr; dKrdT = k.dKrdT; dKrdC = k.dKrdC;
-            viaKc = x.rev == 1;
         } else {
             Kf = lane_kf(M, x, p, logP, logT, invT, &dKfdT);
             if (x.tb >= 0) {
-                const double Mt = s.Mtb[x.tb];
                 dKfdC = Kf;
                 Kf *= Mt;
                 dKfdT *= Mt;
             }
-            viaKc = x.rev != 0;
         }
         if (viaKc) {
             // Kr, dKr/dT and dKr/dM through Kc (JF* reversible branch); the Kc
             // term of dKr/dT is dropped when Kc sits on its clamp
             // (JacobianFunctionI.H:246-249)
-            const double invKc = lane_inv_kc(x, s.B, s.Binv, pf);
-            double sv = s.dBdT[x.sr[0]];
-            #pragma unroll 1
-            for (int q = 1; q < x.nr; q++) sv += s.dBdT[x.sr[q]];
-            double sl = s.dBdT[x.sl[0]];
-            #pragma unroll 1
-            for (int q = 1; q < x.nl; q++) sl += s.dBdT[x.sl[q]];
+            double invKc, sv, sl;
+            if (shortr) {
+                const Tri el = lane_load3(s.B, x.sl), er = lane_load3(s.Binv, x.sr);
+                const Tri gl = lane_load3(s.dBdT, x.sl), gr = lane_load3(s.dBdT, x.sr);
+                invKc = inv_kc3(x, el, er, pf);
+                sv = sum3(gr, x.nr);
+                sl = sum3(gl, x.nl);
+            } else {
+                invKc = lane_inv_kc(x, s.B, s.Binv, pf);
+                sv = s.dBdT[x.sr[0]];
+                #pragma unroll 1
+                for (int q = 1; q < x.nr; q++) sv += s.dBdT[x.sr[q]];
+                sl = s.dBdT[x.sl[0]];
+                #pragma unroll 1
+                for (int q = 1; q < x.nl; q++) sl += s.dBdT[x.sl[q]];
+            }
             const double dKcdTByKc = (sv - sl) - x.dnu * invT;
             Kr = Kf * invKc;
             dKrdT = dKfdT * invKc - (invKc < inv_kc_clamp(x) ? Kr * dKcdTByKc : 0.0);
             dKrdC = dKfdC * invKc;
         }
-        double CF = s.C[x.sl[0]];
-        #pragma unroll 1
-        for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
-        double CR = s.C[x.sr[0]];
-        #pragma unroll 1
-        for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
-        const double qr = Kf * CF - Kr * CR;
-        const double dq = dKfdT * CF - dKrdT * CR;
+        double CF, CR;
+        if (shortr) {
+            CF = prod3(cl, x.nl);
+            CR = prod3(cr, x.nr);
+        } else {
+            CF = s.C[x.sl[0]];
+            #pragma unroll 1
+            for (int q = 1; q < x.nl; q++) CF *= s.C[x.sl[q]];
+            CR = s.C[x.sr[0]];
+            #pragma unroll 1
+            for (int q = 1; q < x.nr; q++) CR *= s.C[x.sr[q]];
+        }
+        s.q[r] = Kf * CF - Kr * CR;
+        s.dq[r] = dKfdT * CF - dKrdT * CR;
         if (x.tb >= 0) s.tbF[x.tb] = dKfdC * CF - dKrdC * CR;
-        #pragma unroll 1
-        for (int q = 0; q < x.nl; q++) {
-            const int i = x.sl[q];
-            f[i] = f[i] - qr;
-            tcAcc[i] = tcAcc[i] - dq;
-        }
-        #pragma unroll 1
-        for (int q = 0; q < x.nr; q++) {
-            const int i = x.sr[q];
-            f[i] = f[i] + qr;
-            tcAcc[i] = tcAcc[i] + dq;
-        }
         // d q / d C_j for each reactant occurrence j: Kf times the other
         // reactant concentrations (the first occurrence of j skipped),
         // scattered down column j to the rows of the reaction
+        const bool dup = repeated_species(x);
         #pragma unroll 1
         for (int qa = 0; qa < x.nl; qa++) {
             const int j = x.sl[qa];
             double d = Kf;
-            bool skipped = false;
-            #pragma unroll 1
-            for (int q = 0; q < x.nl; q++) {
-                if (!skipped && x.sl[q] == j) { skipped = true; continue; }
-                d *= s.C[x.sl[q]];
+            if (shortr && !dup) {
+                // distinct reactants: the occurrence skipped is qa itself
+                if (qa != 0) d *= cl.a;
+                if (qa != 1 && x.nl > 1) d *= cl.b;
+                if (qa != 2 && x.nl > 2) d *= cl.c;
+            } else {
+                bool skipped = false;
+                #pragma unroll 1
+                for (int q = 0; q < x.nl; q++) {
+                    if (!skipped && x.sl[q] == j) { skipped = true; continue; }
+                    d *= s.C[x.sl[q]];
+                }
             }
-            #pragma unroll 1
-            for (int q = 0; q < x.nl; q++) { double& c = J[x.sl[q] * n + j]; c = c - d; }
-            #pragma unroll 1
-            for (int q = 0; q < x.nr; q++) { double& c = J[x.sr[q] * n + j]; c = c + d; }
+            lane_scatter_column(x, J, n, j, d, dup);
         }
         if (x.rev) {
             #pragma unroll 1
             for (int qb = 0; qb < x.nr; qb++) {
                 const int j = x.sr[qb];
                 double d = -Kr;
-                bool skipped = false;
-                #pragma unroll 1
-                for (int q = 0; q < x.nr; q++) {
-                    if (!skipped && x.sr[q] == j) { skipped = true; continue; }
-                    d *= s.C[x.sr[q]];
+                if (shortr && !dup) {
+                    if (qb != 0) d *= cr.a;
+                    if (qb != 1 && x.nr > 1) d *= cr.b;
+                    if (qb != 2 && x.nr > 2) d *= cr.c;
+                } else {
+                    bool skipped = false;
+                    #pragma unroll 1
+                    for (int q = 0; q < x.nr; q++) {
+                        if (!skipped && x.sr[q] == j) { skipped = true; continue; }
+                        d *= s.C[x.sr[q]];
+                    }
                 }
-                #pragma unroll 1
-                for (int q = 0; q < x.nl; q++) { double& c = J[x.sl[q] * n + j]; c = c - d; }
-                #pragma unroll 1
-                for (int q = 0; q < x.nr; q++) { double& c = J[x.sr[q] * n + j]; c = c + d; }
+                lane_scatter_column(x, J, n, j, d, dup);
             }
         }
     }
@@ -355,13 +537,8 @@ __device__ __noinline__ void lane_jac(const DevMech& M, const LaneSlot& s, doubl
         const double w = s.tbF[t];
         const double* eff = M.eff + (size_t)t * ns;
         LA<double> row = J + i * n;
-        if (v & 1) {
-            #pragma unroll 4
-            for (int j = 0; j < ns; j++) row[j] = row[j] + __ldg(&eff[j]) * w;
-        } else {
-            #pragma unroll 4
-            for (int j = 0; j < ns; j++) row[j] = row[j] - __ldg(&eff[j]) * w;
-        }
+        if (v & 1) lane_map(ns, row, [](double a, double b) { return a + b; }, row, LAE{eff, w});
+        else lane_map(ns, row, [](double a, double b) { return a - b; }, row, LAE{eff, w});
     }
     // rows: production rate, temperature column and the dC/dY conversion
     // (diagonal scaling + rank-1 correction)
@@ -369,27 +546,22 @@ __device__ __noinline__ void lane_jac(const DevMech& M, const LaneSlot& s, doubl
     #pragma unroll 1
     for (int i = 0; i < ns; i++) {
         LA<double> row = J + i * n;
-        const double w = f[i], tc = tcAcc[i];
+        const double w = lane_gather(M, s.q, i);
+        const double tc = lane_gather(M, s.dq, i);
         const double WiByrhoM = invRhoM * __ldg(&M.W[i]);
         const double dY = w * WiByrhoM;
         double S = 0;
-        #pragma unroll 4
+        #pragma unroll 8
         for (int k = 0; k < ns; k++) S = fma(row[k], s.C[k], S);
         const double tcol = WiByrhoM * (tc - S * invT) + invT * dY;
         if (fast) {
-            #pragma unroll 4
-            for (int j = 0; j < ns; j++) {
-                const double invWj = __ldg(&M.invW[j]);
-                row[j] = WiByrhoM * (row[j] * (rhoM * invWj)) + (MW * invWj) * dY;
-            }
+            lane_map(ns, row, [=](double a, double invWj) { return WiByrhoM * (a * (rhoM * invWj)) + (MW * invWj) * dY; },
+                     row, LAC{M.invW});
         } else {
             const double K = dY - WiByrhoM * S;
             const double Wi = __ldg(&M.W[i]);
-            #pragma unroll 4
-            for (int j = 0; j < ns; j++) {
-                const double invWj = __ldg(&M.invW[j]);
-                row[j] = fma(row[j], Wi * invWj, (MW * invWj) * K);
-            }
+            lane_map(ns, row, [=](double a, double invWj) { return fma(a, Wi * invWj, (MW * invWj) * K); },
+                     row, LAC{M.invW});
         }
         row[ns] = tcol;
         f[i] = dY;
@@ -401,7 +573,7 @@ __device__ __noinline__ void lane_jac(const DevMech& M, const LaneSlot& s, doubl
     #pragma unroll 1
     for (int j = 0; j < ns; j++) {
         double v = 0;
-        #pragma unroll 4
+        #pragma unroll 8
         for (int i = 0; i < ns; i++) v -= J[i * n + j] * s.Ha[i];
         v -= s.Cp[j] * dTdt;
         J[ns * n + j] = v / CpM;
@@ -415,13 +587,9 @@ __device__ __noinline__ void lane_jac(const DevMech& M, const LaneSlot& s, doubl
 
 // FP64: A = c I - J in place
 __device__ __noinline__ void lane_form_iteration(LA<double> A, int n, double c) {
-    #pragma unroll 1
-    for (int i = 0; i < n; i++) {
-        LA<double> row = A + i * n;
-        #pragma unroll 4
-        for (int j = 0; j < n; j++) row[j] = -row[j];
-        row[i] = row[i] + c;
-    }
+    lane_map(n * n, A, [](double a) { return -a; }, A);
+    #pragma unroll 4
+    for (int i = 0; i < n; i++) { double& d = A[i * n + i]; d = d + c; }
 }
 
 // choose_pivot (LUsolver.C:106-246 panel rules) over a per-lane matrix
@@ -480,65 +648,84 @@ __device__ __noinline__ void lane_lu(LA<double> A, int n, LA<int> piv, LA<double
             piv[k] = pr;
             if (pr != k) {
                 LA<double> rk = A + k * n, rp = A + pr * n;
-                #pragma unroll 4
-                for (int j = 0; j < n; j++) { const double t = rk[j]; rk[j] = rp[j]; rp[j] = t; }
-            }
-            #pragma unroll 4
-            for (int i = k + 1; i < n; i++) A[i * n + k] = A[i * n + k] * rinv;
-            if (k + 1 < k1) {
-                #pragma unroll 1
-                for (int i = k + 1; i < n; i++) {
-                    const double l = A[i * n + k];
-                    #pragma unroll 1
-                    for (int j = k + 1; j < k1; j++) A[i * n + j] = fma(-l, A[k * n + j], A[i * n + j]);
+                int j = 0;
+                for (; j + 4 <= n; j += 4) {
+                    const double a0 = rk[j], a1 = rk[j + 1], a2 = rk[j + 2], a3 = rk[j + 3];
+                    const double b0 = rp[j], b1 = rp[j + 1], b2 = rp[j + 2], b3 = rp[j + 3];
+                    rk[j] = b0; rk[j + 1] = b1; rk[j + 2] = b2; rk[j + 3] = b3;
+                    rp[j] = a0; rp[j + 1] = a1; rp[j + 2] = a2; rp[j + 3] = a3;
                 }
+                #pragma unroll 1
+                for (; j < n; j++) { const double t = rk[j]; rk[j] = rp[j]; rp[j] = t; }
+            }
+            // column k below the diagonal times 1/pivot, then the rest of the
+            // panel's columns in those rows (u: the pivot row's panel entries)
+            const double u1 = k + 1 < k1 ? A[k * n + k + 1] : 0.0;
+            const double u2 = k + 2 < k1 ? A[k * n + k + 2] : 0.0;
+            const double u3 = k + 3 < k1 ? A[k * n + k + 3] : 0.0;
+            const int w = k1 - k - 1;  // remaining panel columns: 0..3
+            #pragma unroll 1
+            for (int i = k + 1; i < n; i++) {
+                LA<double> ri = A + i * n;
+                const double a = ri[k];
+                const double b1 = w > 0 ? ri[k + 1] : 0.0, b2 = w > 1 ? ri[k + 2] : 0.0, b3 = w > 2 ? ri[k + 3] : 0.0;
+                const double l = a * rinv;
+                ri[k] = l;
+                if (w > 0) ri[k + 1] = fma(-l, u1, b1);
+                if (w > 1) ri[k + 2] = fma(-l, u2, b2);
+                if (w > 2) ri[k + 3] = fma(-l, u3, b3);
             }
         }
         if (k1 >= n) break;
         // (b) the panel's U rows in the trailing columns
         #pragma unroll 1
         for (int k = k0 + 1; k < k1; k++) {
+            LA<double> rk = A + k * n;
+            const int nm = k - k0;  // 1..3 earlier panel rows
+            const double l0 = rk[k0], l1 = nm > 1 ? rk[k0 + 1] : 0.0, l2 = nm > 2 ? rk[k0 + 2] : 0.0;
+            const LA<double> m0 = A + k0 * n, m1 = A + (k0 + 1) * n, m2 = A + (k0 + 2) * n;
             #pragma unroll 1
-            for (int m = k0; m < k; m++) {
-                const double l = A[k * n + m];
-                LA<double> rk = A + k * n, rm = A + m * n;
-                #pragma unroll 4
-                for (int j = k1; j < n; j++) rk[j] = fma(-l, rm[j], rk[j]);
+            for (int j = k1; j < n; j += 2) {
+                const bool two = j + 1 < n;
+                const double a0 = rk[j], a1 = two ? rk[j + 1] : 0.0;
+                const double p0 = m0[j], p1 = two ? m0[j + 1] : 0.0;
+                const double q0 = nm > 1 ? m1[j] : 0.0, q1 = nm > 1 && two ? m1[j + 1] : 0.0;
+                const double s0 = nm > 2 ? m2[j] : 0.0, s1 = nm > 2 && two ? m2[j + 1] : 0.0;
+                double r0 = fma(-l0, p0, a0), r1 = fma(-l0, p1, a1);
+                if (nm > 1) { r0 = fma(-l1, q0, r0); r1 = fma(-l1, q1, r1); }
+                if (nm > 2) { r0 = fma(-l2, s0, r0); r1 = fma(-l2, s1, r1); }
+                rk[j] = r0;
+                if (two) rk[j + 1] = r1;
             }
         }
-        // (c) the trailing block: A[i][j] -= sum over the panel's m, in order
+        // (c) the trailing block: A[i][j] -= sum over the panel's m, in order;
+        // two columns per step, all ten loads first
         const LA<double> u0 = A + k0 * n, u1 = A + (k0 + 1) * n;
-        if (size == 4) {
-            const LA<double> u2 = A + (k0 + 2) * n, u3 = A + (k0 + 3) * n;
-            #pragma unroll 1
-            for (int i = k1; i < n; i++) {
-                LA<double> ri = A + i * n;
-                const double l0 = ri[k0], l1 = ri[k0 + 1], l2 = ri[k0 + 2], l3 = ri[k0 + 3];
-                #pragma unroll 2
-                for (int j = k1; j < n; j++) {
-                    double a = ri[j];
-                    a = fma(-l0, u0[j], a);
-                    a = fma(-l1, u1[j], a);
-                    a = fma(-l2, u2[j], a);
-                    a = fma(-l3, u3[j], a);
-                    ri[j] = a;
-                }
+        const LA<double> u2 = A + (k0 + (size > 2 ? 2 : 1)) * n, u3 = A + (k0 + (size > 3 ? 3 : 1)) * n;
+        #pragma unroll 1
+        for (int i = k1; i < n; i++) {
+            LA<double> ri = A + i * n;
+            const double l0 = ri[k0], l1 = ri[k0 + 1];
+            const double l2 = size > 2 ? ri[k0 + 2] : 0.0, l3 = size > 3 ? ri[k0 + 3] : 0.0;
+            int j = k1;
+            for (; j + 2 <= n; j += 2) {
+                const double a0 = ri[j], a1 = ri[j + 1];
+                const double p0 = u0[j], p1 = u0[j + 1], q0 = u1[j], q1 = u1[j + 1];
+                const double s0 = u2[j], s1 = u2[j + 1], t0 = u3[j], t1 = u3[j + 1];
+                double r0 = fma(-l0, p0, a0), r1 = fma(-l0, p1, a1);
+                r0 = fma(-l1, q0, r0); r1 = fma(-l1, q1, r1);
+                if (size > 2) { r0 = fma(-l2, s0, r0); r1 = fma(-l2, s1, r1); }
+                if (size > 3) { r0 = fma(-l3, t0, r0); r1 = fma(-l3, t1, r1); }
+                ri[j] = r0;
+                ri[j + 1] = r1;
             }
-        } else {
-            #pragma unroll 1
-            for (int i = k1; i < n; i++) {
-                LA<double> ri = A + i * n;
-                const double l0 = ri[k0], l1 = ri[k0 + 1];
-                const double l2 = size == 3 ? ri[k0 + 2] : 0.0;
-                const LA<double> u2 = A + (k0 + (size == 3 ? 2 : 1)) * n;
-                #pragma unroll 1
-                for (int j = k1; j < n; j++) {
-                    double a = ri[j];
-                    a = fma(-l0, u0[j], a);
-                    a = fma(-l1, u1[j], a);
-                    if (size == 3) a = fma(-l2, u2[j], a);
-                    ri[j] = a;
-                }
+            if (j < n) {
+                double a = ri[j];
+                a = fma(-l0, u0[j], a);
+                a = fma(-l1, u1[j], a);
+                if (size > 2) a = fma(-l2, u2[j], a);
+                if (size > 3) a = fma(-l3, u3[j], a);
+                ri[j] = a;
             }
         }
         k0 = k1;
@@ -560,7 +747,7 @@ __device__ __noinline__ void lane_lu_solve(const LA<double> A, int n, const LA<i
     for (int i = 1; i < n; i++) {
         const LA<double> ri = A + i * n;
         VT acc = b[i];
-        #pragma unroll 4
+        #pragma unroll 8
         for (int j = 0; j < i; j++) acc = fma(-VT(ri[j]), b[j], acc);
         b[i] = acc;
     }
@@ -568,7 +755,7 @@ __device__ __noinline__ void lane_lu_solve(const LA<double> A, int n, const LA<i
     for (int i = n - 1; i >= 0; i--) {
         const LA<double> ri = A + i * n;
         VT acc = b[i];
-        #pragma unroll 4
+        #pragma unroll 8
         for (int j = n - 1; j > i; j--) acc = fma(-VT(ri[j]), b[j], acc);
         b[i] = acc * VT(invD[i]);
     }
@@ -580,7 +767,7 @@ __device__ __noinline__ void lane_lu_solve(const LA<double> A, int n, const LA<i
 
 __device__ __forceinline__ void lane_jacobian_and_lu(const DevMech& M, const KOpts& o, const LaneSlot& s, double p,
                                                      double cdiag) {
-    lane_jac(M, s, p, s.v(0), s.v(10), s.A, s.v(12), o.jacobian);
+    lane_jac(M, s, p, s.v(0), s.v(10), s.A, o.jacobian);
     lane_form_iteration(s.A, M.n, cdiag);
     lane_lu(s.A, M.n, s.piv, s.invD);
 }
@@ -592,7 +779,7 @@ __device__ __forceinline__ void lane_solve(const LaneSlot& s, int n, LA<double> 
 __device__ __forceinline__ double lane_err_norm(const KOpts& o, int n, const LA<double>& y0, const LA<double>& yt,
                                                 const LA<double>& err) {
     double me = 0;
-    #pragma unroll 1
+    #pragma unroll 4
     for (int i = 0; i < n; i++) {
         const double tol = o.absTol + o.relTol * fmax(fabs(y0[i]), fabs(yt[i]));
         const double e = fabs(err[i]) / tol;
@@ -624,66 +811,55 @@ __device__ __noinline__ double lane_rodas34(const DevMech& M, const KOpts& o, co
     cc.jac++; cc.lu++; cc.rhs += 5; cc.solves += 6;
 
     const double dxd1 = dx * d1 + 1;
-    #pragma unroll 1
-    for (int i = 0; i < n; i++) k1[i] = dxd1 * dfdx[i];
+    lane_map(n, k1, [=](double f) { return dxd1 * f; }, dfdx);
     lane_solve(s, n, k1);
-    #pragma unroll 1
-    for (int i = 0; i < n; i++) yTemp[i] = fma(a21, k1[i], y0[i]);
+    lane_map(n, yTemp, [=](double a, double y) { return fma(a21, a, y); }, k1, y0);
     lane_rhs(M, s, p, yTemp, dydx, 1);
     {
         const double dxd2 = dx * d2, e1 = c21 * invdx;
-        #pragma unroll 1
-        for (int i = 0; i < n; i++) k2[i] = fma(e1, k1[i], fma(dxd2, dfdx[i], dydx[i]));
+        lane_map(n, k2, [=](double a, double f, double g) { return fma(e1, a, fma(dxd2, f, g)); }, k1, dfdx, dydx);
     }
     lane_solve(s, n, k2);
-    #pragma unroll 1
-    for (int i = 0; i < n; i++) yTemp[i] = fma(a32, k2[i], fma(a31, k1[i], y0[i]));
+    lane_map(n, yTemp, [=](double a, double b, double y) { return fma(a32, b, fma(a31, a, y)); }, k1, k2, y0);
     lane_rhs(M, s, p, yTemp, dydx, 1);
     {
         const double dxd3 = dx * d3, e1 = c31 * invdx, e2 = c32 * invdx;
-        #pragma unroll 1
-        for (int i = 0; i < n; i++) k3[i] = fma(e2, k2[i], fma(e1, k1[i], fma(dxd3, dfdx[i], dydx[i])));
+        lane_map(n, k3, [=](double a, double b, double f, double g) { return fma(e2, b, fma(e1, a, fma(dxd3, f, g))); },
+                 k1, k2, dfdx, dydx);
     }
     lane_solve(s, n, k3);
-    #pragma unroll 1
-    for (int i = 0; i < n; i++) yTemp[i] = fma(a43, k3[i], fma(a42, k2[i], fma(a41, k1[i], y0[i])));
+    lane_map(n, yTemp, [=](double a, double b, double c, double y) { return fma(a43, c, fma(a42, b, fma(a41, a, y))); },
+             k1, k2, k3, y0);
     lane_rhs(M, s, p, yTemp, dydx, 1);
     {
         const double dxd4 = dx * d4, e1 = c41 * invdx, e2 = c42 * invdx, e3 = c43 * invdx;
-        #pragma unroll 1
-        for (int i = 0; i < n; i++)
-            k4[i] = fma(e3, k3[i], fma(e2, k2[i], fma(e1, k1[i], fma(dxd4, dfdx[i], dydx[i]))));
+        lane_map(n, k4, [=](double a, double b, double c, double f, double g) {
+            return fma(e3, c, fma(e2, b, fma(e1, a, fma(dxd4, f, g))));
+        }, k1, k2, k3, dfdx, dydx);
     }
     lane_solve(s, n, k4);
-    #pragma unroll 1
-    for (int i = 0; i < n; i++) {
-        const double d = fma(a54, k4[i], fma(a53, k3[i], fma(a52, k2[i], a51 * k1[i])));
-        dy[i] = d;
-        yTemp[i] = y0[i] + d;
-    }
+    lane_map(n, dy, [=](double a, double b, double c, double d) { return fma(a54, d, fma(a53, c, fma(a52, b, a51 * a))); },
+             k1, k2, k3, k4);
+    lane_map(n, yTemp, [](double y, double d) { return y + d; }, y0, dy);
     lane_rhs(M, s, p, yTemp, dydx, 1);
     {
         const double e1 = c51 * invdx, e2 = c52 * invdx, e3 = c53 * invdx, e4 = c54 * invdx;
-        #pragma unroll 1
-        for (int i = 0; i < n; i++) k5[i] = fma(e4, k4[i], fma(e3, k3[i], fma(e2, k2[i], fma(e1, k1[i], dydx[i]))));
+        lane_map(n, k5, [=](double a, double b, double c, double d, double g) {
+            return fma(e4, d, fma(e3, c, fma(e2, b, fma(e1, a, g))));
+        }, k1, k2, k3, k4, dydx);
     }
     lane_solve(s, n, k5);
-    #pragma unroll 1
-    for (int i = 0; i < n; i++) {
-        const double d = dy[i] + k5[i];
-        dy[i] = d;
-        yTemp[i] = y0[i] + d;
-    }
+    lane_map(n, dy, [](double d, double k) { return d + k; }, dy, k5);
+    lane_map(n, yTemp, [](double y, double d) { return y + d; }, y0, dy);
     lane_rhs(M, s, p, yTemp, dydx, 2);
     {
         const double e1 = c61 * invdx, e2 = c62 * invdx, e3 = c63 * invdx, e4 = c64 * invdx, e5 = c65 * invdx;
-        #pragma unroll 1
-        for (int i = 0; i < n; i++)
-            err[i] = fma(e5, k5[i], fma(e4, k4[i], fma(e3, k3[i], fma(e2, k2[i], fma(e1, k1[i], dydx[i])))));
+        lane_map(n, err, [=](double a, double b, double c, double d, double e, double g) {
+            return fma(e5, e, fma(e4, d, fma(e3, c, fma(e2, b, fma(e1, a, g)))));
+        }, k1, k2, k3, k4, k5, dydx);
     }
     lane_solve(s, n, err);
-    #pragma unroll 1
-    for (int i = 0; i < n; i++) yTemp[i] = y0[i] + dy[i] + err[i];
+    lane_map(n, yTemp, [](double y, double d, double e) { return y + d + e; }, y0, dy, err);
     return lane_err_norm(o, n, y0, yTemp, err);
 }
 
@@ -844,6 +1020,7 @@ struct LaneCtl {
     long long c;      // cell, or -1
     double p, deltaT, x, dxTry, dxTry0, dx;
     double sub0;      // the cell's initial sub-step (kept on failure, as ODESolve leaves it)
+    int att;          // attempts on this cell
     int nStep, rejects;
     bool last, retry;
 };
@@ -897,6 +1074,7 @@ lane_integrate_kernel(const DevMech M, const KOpts o, const LaneLayout L, CellIO
                     k.sub0 = io.subDt[c];
                     k.dxTry = k.sub0;
                     k.nStep = 0;
+                    k.att = 0;
                     k.last = false;
                     k.retry = false;
                 }
@@ -921,6 +1099,7 @@ lane_integrate_kernel(const DevMech M, const KOpts o, const LaneLayout L, CellIO
                 // 3. one attempt (the same code on every lane)
                 const double Err = lane_attempt(M, o, s, k.p, k.dx, cc);
                 cc.attempts++;
+                k.att++;
                 // 4. the controller
                 if (Err > 1) {
                     if (++k.rejects > o.maxRejects) {
@@ -935,8 +1114,7 @@ lane_integrate_kernel(const DevMech M, const KOpts o, const LaneLayout L, CellIO
                     cc.accepted++;
                     k.retry = false;
                     k.x += k.dx;
-                    #pragma unroll 1
-                    for (int i = 0; i < n; i++) y[i] = yTemp[i];
+                    lane_map(n, y, [](double v) { return v; }, yTemp);
                     k.dxTry = (Err > ratio) ? fmin(fmax(SAFE * pow(Err, -ALPHA_INC), MIN_SCALE), MAX_SCALE) * k.dx
                                             : safeMaxScale * k.dx;
                     if ((k.x - k.deltaT) * (k.deltaT - 0.0) >= 0) {
@@ -967,6 +1145,7 @@ lane_integrate_kernel(const DevMech M, const KOpts o, const LaneLayout L, CellIO
             dtMin = fmin(dtMin, subDt);
             io.subDt[c] = subDt < o.dtChemMax ? subDt : o.dtChemMax;
             if (io.status) io.status[c] = st;
+            if (io.attempts) io.attempts[c] = k.att;
             k.c = -1;
         }
     }

@@ -14,7 +14,7 @@ namespace fcs {
 constexpr int kLaneVecs = 13;  // stage / work vectors per lane (see fcs_lane.cuh)
 
 struct LaneLayout {
-    int n, ns, nTB;
+    int n, ns, nr, nTB;
     int offA;     // [n*n] FP64 Jacobian / iteration matrix (row-major), LU factors in place (FP64 method)
     int offVec;   // kLaneVecs vectors of n doubles
     int offSp;    // 6 species arrays [ns]: C, B = exp(-G/RT), Binv, Cp, Ha, dB/dT
@@ -24,14 +24,16 @@ struct LaneLayout {
     int offLU32;  // mixed precision: [n*n] FP32 LU factors (n*n/2 rounded up doubles)
     int offScale; // mixed precision: [2n] row and column equilibration factors
     int offX32;   // mixed precision: 2 vectors of n floats (n rounded up doubles)
+    int offRx;    // [2 nr] per-reaction net rate q and its temperature derivative dq/dT
     int words;    // doubles per lane
 };
 
-inline LaneLayout make_lane_layout(int ns, int nTB, bool mixed) {
+inline LaneLayout make_lane_layout(int ns, int nr, int nTB, bool mixed) {
     LaneLayout L;
     const int n = ns + 1;
     L.n = n;
     L.ns = ns;
+    L.nr = nr;
     L.nTB = nTB;
     int o = 0;
     L.offA = o;     o += n * n;
@@ -43,6 +45,7 @@ inline LaneLayout make_lane_layout(int ns, int nTB, bool mixed) {
     L.offLU32 = o;  if (mixed) o += (n * n + 1) / 2;
     L.offScale = o; if (mixed) o += 2 * n;
     L.offX32 = o;   if (mixed) o += n;
+    L.offRx = o;    o += 2 * (nr > 0 ? nr : 1);
     L.words = o;
     return L;
 }

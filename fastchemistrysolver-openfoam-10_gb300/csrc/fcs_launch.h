@@ -22,6 +22,9 @@ struct CellIO {
     int* status;               // may be null
     long long* stats;          // ST_COUNT counters
     unsigned long long* dtMinBits;  // min of the uncapped sub-steps (positive-double bits)
+    int* attempts;             // per cell: attempted steps of its last integration (written; may be null)
+    int attemptsValid;         // attempts[] holds this batch's counts from the previous call: the
+                               // binned queue orders the cells by it (most attempts first)
 };
 
 struct WorkQueue {
@@ -33,7 +36,7 @@ struct WorkQueue {
 
 // Work-queue counters (int) of the binned queue: next position, length,
 // cells per bin, cells placed per bin, and a spare counter for callers.
-constexpr int kQueueBins = 32;
+constexpr int kQueueBins = 64;
 enum { QC_HEAD = 0, QC_LEN = 1, QC_BINS = 2, QC_FILL = QC_BINS + kQueueBins, QC_AUX = QC_FILL + kQueueBins,
        QC_COUNT };
 
@@ -54,8 +57,10 @@ cudaError_t launch_classify(const CellIO& io, int ns, double Treact, int* order,
                             cudaStream_t st);
 cudaError_t integrate_attributes(int group, bool mixed, int* maxThreads, int* regs);
 // Treact skip (as launch_classify) and, for the reacting cells, the bin of
-// their predicted step count delta_t / sub_delta_t (bin = floor(log2), 0..31);
-// bin[c] = -1 for skipped cells.
+// their predicted cost: the attempted steps of their previous integration
+// when io.attemptsValid (bin = floor(8 log2(attempts)) - 24, eight bins per
+// octave from 8 to 2048 attempts), else the step count delta_t / sub_delta_t
+// (bin = floor(log2), 0..31); bin[c] = -1 for skipped cells.
 cudaError_t launch_classify_binned(const CellIO& io, int ns, double Treact, int* bin, int* counters,
                                    cudaStream_t st);
 // order[] = cells with bin >= 0, highest bin first; counters[QC_LEN] = their count.
