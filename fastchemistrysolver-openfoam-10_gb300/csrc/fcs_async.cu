@@ -47,7 +47,7 @@ extern "C" fcs_status fcs_integrate_async(fcs_ctx* ctx, int64_t nc, double dt, c
     if (sorted) CK(ctx->bBin.ensure(std::max<int64_t>(nc, 1)));
     if (!ctx->hStats) CK(cudaMallocHost(&ctx->hStats, (ST_COUNT + 1) * sizeof(long long)));
     if (!ctx->evAsync) CK(cudaEventCreateWithFlags(&ctx->evAsync, cudaEventDisableTiming));
-    const int group = cached_group(ctx);
+    const int group = lane_auto(ctx, nc) ? (int)FCS_MAPPING_LANE : cached_group(ctx);
     Shape sh;
     if (!make_shape(ctx, group, true, sh)) return set_err(ctx, FCS_ERR_UNSUPPORTED, "no launch shape for this mapping");
     fcs_status s = ensure_gws(ctx, sh);

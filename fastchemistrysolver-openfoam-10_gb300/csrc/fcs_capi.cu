@@ -389,22 +389,25 @@ KOpts fcs::kopts(const fcs_options& o) {
 
 // Lane per cell (FCS_MAPPING_LANE): blocks of 128 threads, as many per SM
 // as the registers allow (at most 4), a global-memory workspace of
-// make_lane_layout(...).words doubles per thread.  Rosenbrock-family solvers
-// in FP64 only.
+// make_lane_layout(...).words doubles per thread.  Rosenbrock-family solvers,
+// FP64 or mixed precision.
 static bool make_lane_shape(fcs_ctx* ctx, bool integrate, Shape& sh) {
     const fcs_options& o = ctx->opt;
     const bool mixed = o.precision == FCS_PRECISION_MIXED;
-    if (!integrate || o.solver == FCS_SOLVER_SEULEX || mixed) return false;
+    if (!integrate || o.solver == FCS_SOLVER_SEULEX) return false;
     int maxThreads = 0, regs = 0;
     if (integrate_attributes(1, mixed, &maxThreads, &regs) != cudaSuccess) return false;
     constexpr int kBlock = 128;
     if (maxThreads < kBlock) return false;
-    int perSM = std::max(1, std::min(4, 65536 / std::max(1, regs * kBlock)));
-    // FCS_LANE_BLOCKS_PER_SM caps the resident blocks (fewer lanes than cells
-    // lets lanes take several cells each and balance uneven cells)
+    const int maxPerSM = std::max(1, std::min(4, 65536 / std::max(1, regs * kBlock)));
+    // Three resident blocks (12 warps) per SM by default: on the 53-species
+    // field (65,536 cells) 3 blocks ran 5,531 cells/s against 5,311 with 4
+    // and 4,970 with 2 -- fewer lanes than cells let the lanes that finish
+    // early take the remaining cells.  FCS_LANE_BLOCKS_PER_SM overrides it.
+    int perSM = std::min(3, maxPerSM);
     if (const char* e = std::getenv("FCS_LANE_BLOCKS_PER_SM")) {
         const int v = std::atoi(e);
-        if (v >= 1) perSM = std::min(perSM, v);
+        if (v >= 1) perSM = std::min(maxPerSM, v);
     }
     sh.mixed = mixed;
     sh.global = true;
@@ -479,6 +482,16 @@ int fcs::default_group(fcs_ctx* ctx) {
     const int n = ctx->M.n;
     if (n <= 128) return 64;
     return 128;
+}
+
+// AUTO chooses the lane mapping for a Rosenbrock-family FP64 step with cells
+// enough to occupy most of its lanes (at fewer cells its lanes idle and the
+// cell groups, which spread one cell over many threads, are faster).
+bool fcs::lane_auto(fcs_ctx* ctx, long long cells) {
+    if (ctx->opt.mapping != FCS_MAPPING_AUTO) return false;
+    Shape sh;
+    if (!make_shape(ctx, FCS_MAPPING_LANE, true, sh)) return false;
+    return cells * 4 >= 3LL * sh.lc.grid * sh.lc.block;
 }
 
 int fcs::cached_group(fcs_ctx* ctx) {
@@ -631,7 +644,7 @@ static fcs_status integrate_impl(fcs_ctx* ctx, int64_t nc, double dt, const doub
         if (!ctx->hStats) CK(cudaMallocHost(&ctx->hStats, (ST_COUNT + 1) * sizeof(long long)));
         hs = ctx->hStats;
         hmin = reinterpret_cast<unsigned long long*>(ctx->hStats + ST_COUNT);
-        group = ctx->opt.mapping ? ctx->opt.mapping : [&] {
+        group = ctx->opt.mapping ? ctx->opt.mapping : lane_auto(ctx, nc) ? (int)FCS_MAPPING_LANE : [&] {
             const auto it = ctx->tuned.find(std::make_tuple(ctx->M.n, (int)ctx->opt.precision, (int)ctx->opt.solver,
                                                             (int)ctx->opt.jacobian));
             return it != ctx->tuned.end() ? it->second : default_group(ctx);
@@ -682,7 +695,8 @@ static fcs_status integrate_impl(fcs_ctx* ctx, int64_t nc, double dt, const doub
         int nActive = 0;
         CK(cudaMemcpyAsync(&nActive, ctx->bHead.p + QC_LEN, sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        group = ctx->opt.mapping ? ctx->opt.mapping : tuned_group(ctx, io, nActive);
+        group = ctx->opt.mapping ? ctx->opt.mapping
+                                 : lane_auto(ctx, nActive) ? (int)FCS_MAPPING_LANE : tuned_group(ctx, io, nActive);
         Shape sh;
         if (!make_shape(ctx, group, true, sh))
             return set_err(ctx, FCS_ERR_UNSUPPORTED, "no launch shape for this mapping");

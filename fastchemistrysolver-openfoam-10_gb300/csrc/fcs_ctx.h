@@ -124,6 +124,8 @@ bool make_shape(fcs_ctx* ctx, int group, bool integrate, Shape& sh);
 int default_group(fcs_ctx* ctx);
 // The option's mapping, else one the autotuner cached for this key, else the default.
 int cached_group(fcs_ctx* ctx);
+// AUTO mapping: the lane mapping for this many reacting cells?
+bool lane_auto(fcs_ctx* ctx, long long cells);
 // Global-memory workspace for shapes whose slot exceeds shared memory.
 fcs_status ensure_gws(fcs_ctx* ctx, const Shape& sh);
 

@@ -238,8 +238,9 @@ __global__ void audit_kernel(int ns, long long nc, int cap, const int* counters,
 
 extern "C" fcs_status fcs_gate_default_options(fcs_gate_options* o) {
     if (!o) return FCS_ERR_INVALID;
-    o->T_rel = 2e-4;
-    o->Y_abs = 2e-7;
+    // the method's accuracy target: 1e-3 relative in T, 1e-6 absolute in every Y_i
+    o->T_rel = 1e-3;
+    o->Y_abs = 1e-6;
     o->element_abs = 1e-6;
     o->audit_fraction = 0.02;
     o->seed_substep = 1;
@@ -347,7 +348,8 @@ extern "C" fcs_status fcs_integrate_gated(fcs_ctx* ctx, int64_t nc, double dt, c
     CK(cudaMemsetAsync(ctx->bHead.p, 0, 2 * sizeof(int), st));
     CK(cudaMemsetAsync(g->counters.p, 0, QC_COUNT * sizeof(int), st));
     CK(cudaMemsetAsync(g->gstats.p, 0, GS_COUNT * sizeof(unsigned long long), st));
-    const int group = ctx->opt.mapping ? ctx->opt.mapping : [&] {
+    // the fallback cells run with the plain method's mapping for this batch
+    const int group = ctx->opt.mapping ? ctx->opt.mapping : lane_auto(ctx, nc) ? (int)FCS_MAPPING_LANE : [&] {
         const auto key = std::make_tuple(ctx->M.n, (int)ctx->opt.precision, (int)ctx->opt.solver, (int)ctx->opt.jacobian);
         const auto it = ctx->tuned.find(key);
         return it != ctx->tuned.end() ? it->second : default_group(ctx);

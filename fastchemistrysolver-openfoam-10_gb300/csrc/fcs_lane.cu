@@ -5,9 +5,9 @@ namespace fcs {
 
 cudaError_t launch_lane_integrate(const LaunchCfg& lc, bool mixed, const DevMech& M, const KOpts& o,
                                   const CellIO& io, const WorkQueue& q, char* gws, cudaStream_t st) {
-    if (mixed || !gws || lc.block % 32 != 0) return cudaErrorInvalidValue;
-    const LaneLayout L = make_lane_layout(M.ns, M.nr, M.nTB, false);
-    auto k = lane_integrate_kernel<double>;
+    if (!gws || lc.block % 32 != 0) return cudaErrorInvalidValue;
+    const LaneLayout L = make_lane_layout(M.ns, M.nr, M.nTB, mixed);
+    auto k = mixed ? lane_integrate_kernel<float> : lane_integrate_kernel<double>;
     // the workspace lives in global memory: all of the unified L1/shared
     // memory as L1, which caches the lanes' vectors and species arrays
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -18,9 +18,8 @@ cudaError_t launch_lane_integrate(const LaunchCfg& lc, bool mixed, const DevMech
 }
 
 cudaError_t lane_attributes(bool mixed, int* maxThreads, int* regs) {
-    if (mixed) return cudaErrorInvalidValue;
     cudaFuncAttributes a;
-    cudaError_t e = cudaFuncGetAttributes(&a, lane_integrate_kernel<double>);
+    cudaError_t e = cudaFuncGetAttributes(&a, mixed ? lane_integrate_kernel<float> : lane_integrate_kernel<double>);
     if (e != cudaSuccess) return e;
     *maxThreads = a.maxThreadsPerBlock;
     *regs = a.numRegs;

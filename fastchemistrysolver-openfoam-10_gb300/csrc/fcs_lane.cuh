@@ -593,7 +593,8 @@ __device__ __noinline__ void lane_form_iteration(LA<double> A, int n, double c) 
 }
 
 // choose_pivot (LUsolver.C:106-246 panel rules) over a per-lane matrix
-__device__ __forceinline__ int lane_choose_pivot(const LA<double>& A, int n, int k, int pos, int size) {
+template<class T>
+__device__ __forceinline__ int lane_choose_pivot(const LA<T>& A, int n, int k, int pos, int size) {
     const int cand = size - pos;
     if (cand <= 1) return k;
     if (pos == 0 && size >= 3) {
@@ -601,21 +602,21 @@ __device__ __forceinline__ int lane_choose_pivot(const LA<double>& A, int n, int
         double t = 0;
         #pragma unroll 1
         for (int c = 0; c < size; c++) {
-            const double v = fabs(A[(k + c) * n + k]);
+            const double v = fabs(double(A[(k + c) * n + k]));
             if (t < v) { best = c; t = v; }
         }
         return k + best;
     }
     if (size == 4 && pos == 1) {
         // LUsolver.C:169-185: the running maximum keeps the signed value of row 2
-        double t = fabs(A[k * n + k]);
+        double t = fabs(double(A[k * n + k]));
         int best = 0;
-        const double v1 = A[(k + 1) * n + k];
+        const double v1 = double(A[(k + 1) * n + k]);
         if (t < fabs(v1)) { best = 1; t = v1; }
-        if (t < fabs(A[(k + 2) * n + k])) best = 2;
+        if (t < fabs(double(A[(k + 2) * n + k]))) best = 2;
         return k + best;
     }
-    return (fabs(A[k * n + k]) < fabs(A[(k + 1) * n + k])) ? k + 1 : k;
+    return (fabs(double(A[k * n + k])) < fabs(double(A[(k + 1) * n + k]))) ? k + 1 : k;
 }
 
 // LU with the reference's panel-local pivoting (LUsolver.C:106-246,
@@ -623,7 +624,10 @@ __device__ __forceinline__ int lane_choose_pivot(const LA<double>& A, int n, int
 // columns are factored and updated eagerly, the panel's U rows and the
 // trailing block receive the panel's rank-4 update afterwards, each element
 // in the same multiply-add order as the column-by-column factorisation.
-__device__ __noinline__ void lane_lu(LA<double> A, int n, LA<int> piv, LA<double> invD) {
+// T: double (FP64 method) or float (the mixed method's FP32 factors; the
+// reciprocal pivots are kept in double, rounded to float as in the cell groups).
+template<class T>
+__device__ __noinline__ void lane_lu(LA<T> A, int n, LA<int> piv, LA<double> invD) {
     const int rem = n & 3;
     int k0 = 0;
     #pragma unroll 1
@@ -631,7 +635,7 @@ __device__ __noinline__ void lane_lu(LA<double> A, int n, LA<int> piv, LA<double
         const bool tail = k0 >= n - rem;
         const int size = tail ? rem : 4;
         if (size == 1) {
-            invD[k0] = 1.0 / A[k0 * n + k0];
+            invD[k0] = 1.0 / double(A[k0 * n + k0]);
             piv[k0] = k0;
             break;
         }
@@ -641,35 +645,35 @@ __device__ __noinline__ void lane_lu(LA<double> A, int n, LA<int> piv, LA<double
         for (int k = k0; k < k1; k++) {
             const int pos = k - k0;
             const int pr = lane_choose_pivot(A, n, k, pos, size);
-            double akk = A[pr * n + k];
+            double akk = double(A[pr * n + k]);
             if (akk == 0) akk = kPivEps;
-            const double rinv = 1.0 / akk;
-            invD[k] = rinv;
+            const T rinv = T(1.0 / akk);
+            invD[k] = double(rinv);
             piv[k] = pr;
             if (pr != k) {
-                LA<double> rk = A + k * n, rp = A + pr * n;
+                LA<T> rk = A + k * n, rp = A + pr * n;
                 int j = 0;
                 for (; j + 4 <= n; j += 4) {
-                    const double a0 = rk[j], a1 = rk[j + 1], a2 = rk[j + 2], a3 = rk[j + 3];
-                    const double b0 = rp[j], b1 = rp[j + 1], b2 = rp[j + 2], b3 = rp[j + 3];
+                    const T a0 = rk[j], a1 = rk[j + 1], a2 = rk[j + 2], a3 = rk[j + 3];
+                    const T b0 = rp[j], b1 = rp[j + 1], b2 = rp[j + 2], b3 = rp[j + 3];
                     rk[j] = b0; rk[j + 1] = b1; rk[j + 2] = b2; rk[j + 3] = b3;
                     rp[j] = a0; rp[j + 1] = a1; rp[j + 2] = a2; rp[j + 3] = a3;
                 }
                 #pragma unroll 1
-                for (; j < n; j++) { const double t = rk[j]; rk[j] = rp[j]; rp[j] = t; }
+                for (; j < n; j++) { const T t = rk[j]; rk[j] = rp[j]; rp[j] = t; }
             }
             // column k below the diagonal times 1/pivot, then the rest of the
             // panel's columns in those rows (u: the pivot row's panel entries)
-            const double u1 = k + 1 < k1 ? A[k * n + k + 1] : 0.0;
-            const double u2 = k + 2 < k1 ? A[k * n + k + 2] : 0.0;
-            const double u3 = k + 3 < k1 ? A[k * n + k + 3] : 0.0;
+            const T u1 = k + 1 < k1 ? A[k * n + k + 1] : T(0);
+            const T u2 = k + 2 < k1 ? A[k * n + k + 2] : T(0);
+            const T u3 = k + 3 < k1 ? A[k * n + k + 3] : T(0);
             const int w = k1 - k - 1;  // remaining panel columns: 0..3
             #pragma unroll 1
             for (int i = k + 1; i < n; i++) {
-                LA<double> ri = A + i * n;
-                const double a = ri[k];
-                const double b1 = w > 0 ? ri[k + 1] : 0.0, b2 = w > 1 ? ri[k + 2] : 0.0, b3 = w > 2 ? ri[k + 3] : 0.0;
-                const double l = a * rinv;
+                LA<T> ri = A + i * n;
+                const T a = ri[k];
+                const T b1 = w > 0 ? ri[k + 1] : T(0), b2 = w > 1 ? ri[k + 2] : T(0), b3 = w > 2 ? ri[k + 3] : T(0);
+                const T l = a * rinv;
                 ri[k] = l;
                 if (w > 0) ri[k + 1] = fma(-l, u1, b1);
                 if (w > 1) ri[k + 2] = fma(-l, u2, b2);
@@ -680,18 +684,18 @@ __device__ __noinline__ void lane_lu(LA<double> A, int n, LA<int> piv, LA<double
         // (b) the panel's U rows in the trailing columns
         #pragma unroll 1
         for (int k = k0 + 1; k < k1; k++) {
-            LA<double> rk = A + k * n;
+            LA<T> rk = A + k * n;
             const int nm = k - k0;  // 1..3 earlier panel rows
-            const double l0 = rk[k0], l1 = nm > 1 ? rk[k0 + 1] : 0.0, l2 = nm > 2 ? rk[k0 + 2] : 0.0;
-            const LA<double> m0 = A + k0 * n, m1 = A + (k0 + 1) * n, m2 = A + (k0 + 2) * n;
+            const T l0 = rk[k0], l1 = nm > 1 ? rk[k0 + 1] : T(0), l2 = nm > 2 ? rk[k0 + 2] : T(0);
+            const LA<T> m0 = A + k0 * n, m1 = A + (k0 + 1) * n, m2 = A + (k0 + 2) * n;
             #pragma unroll 1
             for (int j = k1; j < n; j += 2) {
                 const bool two = j + 1 < n;
-                const double a0 = rk[j], a1 = two ? rk[j + 1] : 0.0;
-                const double p0 = m0[j], p1 = two ? m0[j + 1] : 0.0;
-                const double q0 = nm > 1 ? m1[j] : 0.0, q1 = nm > 1 && two ? m1[j + 1] : 0.0;
-                const double s0 = nm > 2 ? m2[j] : 0.0, s1 = nm > 2 && two ? m2[j + 1] : 0.0;
-                double r0 = fma(-l0, p0, a0), r1 = fma(-l0, p1, a1);
+                const T a0 = rk[j], a1 = two ? rk[j + 1] : T(0);
+                const T p0 = m0[j], p1 = two ? m0[j + 1] : T(0);
+                const T q0 = nm > 1 ? m1[j] : T(0), q1 = nm > 1 && two ? m1[j + 1] : T(0);
+                const T s0 = nm > 2 ? m2[j] : T(0), s1 = nm > 2 && two ? m2[j + 1] : T(0);
+                T r0 = fma(-l0, p0, a0), r1 = fma(-l0, p1, a1);
                 if (nm > 1) { r0 = fma(-l1, q0, r0); r1 = fma(-l1, q1, r1); }
                 if (nm > 2) { r0 = fma(-l2, s0, r0); r1 = fma(-l2, s1, r1); }
                 rk[j] = r0;
@@ -700,19 +704,19 @@ __device__ __noinline__ void lane_lu(LA<double> A, int n, LA<int> piv, LA<double
         }
         // (c) the trailing block: A[i][j] -= sum over the panel's m, in order;
         // two columns per step, all ten loads first
-        const LA<double> u0 = A + k0 * n, u1 = A + (k0 + 1) * n;
-        const LA<double> u2 = A + (k0 + (size > 2 ? 2 : 1)) * n, u3 = A + (k0 + (size > 3 ? 3 : 1)) * n;
+        const LA<T> u0 = A + k0 * n, u1 = A + (k0 + 1) * n;
+        const LA<T> u2 = A + (k0 + (size > 2 ? 2 : 1)) * n, u3 = A + (k0 + (size > 3 ? 3 : 1)) * n;
         #pragma unroll 1
         for (int i = k1; i < n; i++) {
-            LA<double> ri = A + i * n;
-            const double l0 = ri[k0], l1 = ri[k0 + 1];
-            const double l2 = size > 2 ? ri[k0 + 2] : 0.0, l3 = size > 3 ? ri[k0 + 3] : 0.0;
+            LA<T> ri = A + i * n;
+            const T l0 = ri[k0], l1 = ri[k0 + 1];
+            const T l2 = size > 2 ? ri[k0 + 2] : T(0), l3 = size > 3 ? ri[k0 + 3] : T(0);
             int j = k1;
             for (; j + 2 <= n; j += 2) {
-                const double a0 = ri[j], a1 = ri[j + 1];
-                const double p0 = u0[j], p1 = u0[j + 1], q0 = u1[j], q1 = u1[j + 1];
-                const double s0 = u2[j], s1 = u2[j + 1], t0 = u3[j], t1 = u3[j + 1];
-                double r0 = fma(-l0, p0, a0), r1 = fma(-l0, p1, a1);
+                const T a0 = ri[j], a1 = ri[j + 1];
+                const T p0 = u0[j], p1 = u0[j + 1], q0 = u1[j], q1 = u1[j + 1];
+                const T s0 = u2[j], s1 = u2[j + 1], t0 = u3[j], t1 = u3[j + 1];
+                T r0 = fma(-l0, p0, a0), r1 = fma(-l0, p1, a1);
                 r0 = fma(-l1, q0, r0); r1 = fma(-l1, q1, r1);
                 if (size > 2) { r0 = fma(-l2, s0, r0); r1 = fma(-l2, s1, r1); }
                 if (size > 3) { r0 = fma(-l3, t0, r0); r1 = fma(-l3, t1, r1); }
@@ -720,7 +724,7 @@ __device__ __noinline__ void lane_lu(LA<double> A, int n, LA<int> piv, LA<double
                 ri[j + 1] = r1;
             }
             if (j < n) {
-                double a = ri[j];
+                T a = ri[j];
                 a = fma(-l0, u0[j], a);
                 a = fma(-l1, u1[j], a);
                 if (size > 2) a = fma(-l2, u2[j], a);
@@ -735,8 +739,8 @@ __device__ __noinline__ void lane_lu(LA<double> A, int n, LA<int> piv, LA<double
 // Forward / back substitution with the factors of lane_lu (LUsolver.C:3145-3171,
 // 4113-4152): the recorded interchanges, unit-lower forward sweep, upper
 // backward sweep times the reciprocal pivots; in place on b.
-template<class VT>
-__device__ __noinline__ void lane_lu_solve(const LA<double> A, int n, const LA<int> piv, const LA<double> invD,
+template<class MT, class VT>
+__device__ __noinline__ void lane_lu_solve(const LA<MT> A, int n, const LA<int> piv, const LA<double> invD,
                                            LA<VT> b) {
     #pragma unroll 1
     for (int j = 0; j < n; j++) {
@@ -745,7 +749,7 @@ __device__ __noinline__ void lane_lu_solve(const LA<double> A, int n, const LA<i
     }
     #pragma unroll 1
     for (int i = 1; i < n; i++) {
-        const LA<double> ri = A + i * n;
+        const LA<MT> ri = A + i * n;
         VT acc = b[i];
         #pragma unroll 8
         for (int j = 0; j < i; j++) acc = fma(-VT(ri[j]), b[j], acc);
@@ -753,7 +757,7 @@ __device__ __noinline__ void lane_lu_solve(const LA<double> A, int n, const LA<i
     }
     #pragma unroll 1
     for (int i = n - 1; i >= 0; i--) {
-        const LA<double> ri = A + i * n;
+        const LA<MT> ri = A + i * n;
         VT acc = b[i];
         #pragma unroll 8
         for (int j = n - 1; j > i; j--) acc = fma(-VT(ri[j]), b[j], acc);
@@ -765,15 +769,106 @@ __device__ __noinline__ void lane_lu_solve(const LA<double> A, int n, const LA<i
 // Rosenbrock attempts, per lane (same stage arithmetic as fcs_kernels.cuh).
 // Vectors: 0 y0, 1 yTemp, 2..6 k1..k5, 7 dy, 8 err, 9 dydx, 10 dfdx, 11 tmp, 12 tcAcc
 
-__device__ __forceinline__ void lane_jacobian_and_lu(const DevMech& M, const KOpts& o, const LaneSlot& s, double p,
-                                                     double cdiag) {
-    lane_jac(M, s, p, s.v(0), s.v(10), s.A, o.jacobian);
-    lane_form_iteration(s.A, M.n, cdiag);
-    lane_lu(s.A, M.n, s.piv, s.invD);
+// Mixed precision: the FP32 factors of Dr (c I - J) Dc with power-of-two row
+// and column equilibration (Dr, Dc in s.dr / s.dc); one narrowing per
+// element, the scaling exact.
+__device__ __noinline__ void lane_form32(const LaneSlot& s, int n) {
+    const LA<double> A = s.A;
+    const LA<float> L = s.LU32;
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) {
+        float mx = 0.f;
+        int j = 0;
+        for (; j + 4 <= n; j += 4) {
+            const double a0 = A[i * n + j], a1 = A[i * n + j + 1], a2 = A[i * n + j + 2], a3 = A[i * n + j + 3];
+            const float b0 = float(a0), b1 = float(a1), b2 = float(a2), b3 = float(a3);
+            L[i * n + j] = b0; L[i * n + j + 1] = b1; L[i * n + j + 2] = b2; L[i * n + j + 3] = b3;
+            mx = fmaxf(mx, fmaxf(fmaxf(fabsf(b0), fabsf(b1)), fmaxf(fabsf(b2), fabsf(b3))));
+        }
+        #pragma unroll 1
+        for (; j < n; j++) {
+            const float b = float(A[i * n + j]);
+            L[i * n + j] = b;
+            mx = fmaxf(mx, fabsf(b));
+        }
+        s.dr[i] = double(pow2_inverse(mx));
+    }
+    #pragma unroll 1
+    for (int j = 0; j < n; j++) {
+        float mx = 0.f;
+        #pragma unroll 4
+        for (int i = 0; i < n; i++) mx = fmaxf(mx, fabsf(L[i * n + j] * float(s.dr[i])));
+        s.dc[j] = double(pow2_inverse(mx));
+    }
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) {
+        const float ri = float(s.dr[i]);
+        int j = 0;
+        for (; j + 4 <= n; j += 4) {
+            const float a0 = L[i * n + j], a1 = L[i * n + j + 1], a2 = L[i * n + j + 2], a3 = L[i * n + j + 3];
+            const float c0 = float(s.dc[j]), c1 = float(s.dc[j + 1]), c2 = float(s.dc[j + 2]), c3 = float(s.dc[j + 3]);
+            L[i * n + j] = a0 * ri * c0; L[i * n + j + 1] = a1 * ri * c1;
+            L[i * n + j + 2] = a2 * ri * c2; L[i * n + j + 3] = a3 * ri * c3;
+        }
+        #pragma unroll 1
+        for (; j < n; j++) L[i * n + j] = L[i * n + j] * ri * float(s.dc[j]);
+    }
 }
 
-__device__ __forceinline__ void lane_solve(const LaneSlot& s, int n, LA<double> b) {
-    lane_lu_solve<double>(s.A, n, s.piv, s.invD, b);
+// Mixed solve (as the cell groups' linear_solve_mixed): x0 = Dc LU32^-1 Dr b in
+// FP32, r = b - A64 x0 in FP64, x = x0 + Dc LU32^-1 Dr r.  False when the
+// correction is not below 1e-3 of the solution (or not finite): the attempt
+// is then redone in FP64.
+__device__ __noinline__ bool lane_solve_mixed(const LaneSlot& s, int n, LA<double> b, LA<double> tmp) {
+    const LA<float> x32 = s.x32, r32 = s.x32 + n;
+    #pragma unroll 4
+    for (int i = 0; i < n; i++) x32[i] = float(b[i] * s.dr[i]);
+    lane_lu_solve<float, float>(s.LU32, n, s.piv, s.invD, x32);
+    #pragma unroll 4
+    for (int i = 0; i < n; i++) tmp[i] = double(x32[i]) * s.dc[i];
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) {
+        const LA<double> Ai = s.A + i * n;
+        double r = b[i];
+        #pragma unroll 8
+        for (int j = 0; j < n; j++) r = fma(-Ai[j], tmp[j], r);
+        r32[i] = float(r * s.dr[i]);
+    }
+    lane_lu_solve<float, float>(s.LU32, n, s.piv, s.invD, r32);
+    double dmax = 0, xmax = 0;
+    #pragma unroll 1
+    for (int i = 0; i < n; i++) {
+        const double d = double(r32[i]) * s.dc[i];
+        const double x = tmp[i] + d;
+        b[i] = x;
+        dmax = fmax(dmax, fabs(d));
+        xmax = fmax(xmax, fabs(x));
+        if (!(d == d) || !(x == x)) dmax = 1e300;
+    }
+    return dmax <= kRefineTol * xmax && xmax < 1e300;
+}
+
+// The iteration matrix of an attempt: the FP64 Jacobian, A = c I - J in
+// FP64, factored in FP64 (the FP64 method, or a mixed attempt redone in
+// FP64) or in FP32 from its equilibrated copy (MIXED).
+template<bool MIXED>
+__device__ __forceinline__ void lane_jacobian_and_lu(const DevMech& M, const KOpts& o, const LaneSlot& s, double p,
+                                                     double cdiag, bool fp64) {
+    lane_jac(M, s, p, s.v(0), s.v(10), s.A, o.jacobian);
+    lane_form_iteration(s.A, M.n, cdiag);
+    if (MIXED && !fp64) {
+        lane_form32(s, M.n);
+        lane_lu<float>(s.LU32, M.n, s.piv, s.invD);
+    } else {
+        lane_lu<double>(s.A, M.n, s.piv, s.invD);
+    }
+}
+
+template<bool MIXED>
+__device__ __forceinline__ bool lane_solve(const LaneSlot& s, int n, LA<double> b, bool fp64) {
+    if (MIXED && !fp64) return lane_solve_mixed(s, n, b, s.v(11));
+    lane_lu_solve<double, double>(s.A, n, s.piv, s.invD, b);
+    return true;
 }
 
 __device__ __forceinline__ double lane_err_norm(const KOpts& o, int n, const LA<double>& y0, const LA<double>& yt,
@@ -789,8 +884,9 @@ __device__ __forceinline__ double lane_err_norm(const KOpts& o, int n, const LA<
 }
 
 // OptRodas34::Rodas34Solve (OptRodas34.C:291-882), constants OptRodas34.H:105-149
+template<bool MIXED>
 __device__ __noinline__ double lane_rodas34(const DevMech& M, const KOpts& o, const LaneSlot& s, double p, double dx,
-                                            double invdx, CellCounters& cc) {
+                                            double invdx, CellCounters& cc, bool fp64) {
     const int n = M.n;
     const LA<double> y0 = s.v(0), yTemp = s.v(1), k1 = s.v(2), k2 = s.v(3), k3 = s.v(4), k4 = s.v(5);
     const LA<double> k5 = s.v(6), dy = s.v(7), err = s.v(8), dydx = s.v(9), dfdx = s.v(10);
@@ -807,19 +903,19 @@ __device__ __noinline__ double lane_rodas34(const DevMech& M, const KOpts& o, co
                  c64 = 0.1631930543123136e2, c65 = -0.6058818238834054e1;
     const double invgamma = 1.0 / 0.25;
     const double cdiag = 1.0 * invdx * invgamma;
-    lane_jacobian_and_lu(M, o, s, p, cdiag);
+    lane_jacobian_and_lu<MIXED>(M, o, s, p, cdiag, fp64);
     cc.jac++; cc.lu++; cc.rhs += 5; cc.solves += 6;
 
     const double dxd1 = dx * d1 + 1;
     lane_map(n, k1, [=](double f) { return dxd1 * f; }, dfdx);
-    lane_solve(s, n, k1);
+    if (!lane_solve<MIXED>(s, n, k1, fp64)) return -1.0;
     lane_map(n, yTemp, [=](double a, double y) { return fma(a21, a, y); }, k1, y0);
     lane_rhs(M, s, p, yTemp, dydx, 1);
     {
         const double dxd2 = dx * d2, e1 = c21 * invdx;
         lane_map(n, k2, [=](double a, double f, double g) { return fma(e1, a, fma(dxd2, f, g)); }, k1, dfdx, dydx);
     }
-    lane_solve(s, n, k2);
+    if (!lane_solve<MIXED>(s, n, k2, fp64)) return -1.0;
     lane_map(n, yTemp, [=](double a, double b, double y) { return fma(a32, b, fma(a31, a, y)); }, k1, k2, y0);
     lane_rhs(M, s, p, yTemp, dydx, 1);
     {
@@ -827,7 +923,7 @@ __device__ __noinline__ double lane_rodas34(const DevMech& M, const KOpts& o, co
         lane_map(n, k3, [=](double a, double b, double f, double g) { return fma(e2, b, fma(e1, a, fma(dxd3, f, g))); },
                  k1, k2, dfdx, dydx);
     }
-    lane_solve(s, n, k3);
+    if (!lane_solve<MIXED>(s, n, k3, fp64)) return -1.0;
     lane_map(n, yTemp, [=](double a, double b, double c, double y) { return fma(a43, c, fma(a42, b, fma(a41, a, y))); },
              k1, k2, k3, y0);
     lane_rhs(M, s, p, yTemp, dydx, 1);
@@ -837,7 +933,7 @@ __device__ __noinline__ double lane_rodas34(const DevMech& M, const KOpts& o, co
             return fma(e3, c, fma(e2, b, fma(e1, a, fma(dxd4, f, g))));
         }, k1, k2, k3, dfdx, dydx);
     }
-    lane_solve(s, n, k4);
+    if (!lane_solve<MIXED>(s, n, k4, fp64)) return -1.0;
     lane_map(n, dy, [=](double a, double b, double c, double d) { return fma(a54, d, fma(a53, c, fma(a52, b, a51 * a))); },
              k1, k2, k3, k4);
     lane_map(n, yTemp, [](double y, double d) { return y + d; }, y0, dy);
@@ -848,7 +944,7 @@ __device__ __noinline__ double lane_rodas34(const DevMech& M, const KOpts& o, co
             return fma(e4, d, fma(e3, c, fma(e2, b, fma(e1, a, g))));
         }, k1, k2, k3, k4, dydx);
     }
-    lane_solve(s, n, k5);
+    if (!lane_solve<MIXED>(s, n, k5, fp64)) return -1.0;
     lane_map(n, dy, [](double d, double k) { return d + k; }, dy, k5);
     lane_map(n, yTemp, [](double y, double d) { return y + d; }, y0, dy);
     lane_rhs(M, s, p, yTemp, dydx, 2);
@@ -858,14 +954,15 @@ __device__ __noinline__ double lane_rodas34(const DevMech& M, const KOpts& o, co
             return fma(e5, e, fma(e4, d, fma(e3, c, fma(e2, b, fma(e1, a, g)))));
         }, k1, k2, k3, k4, k5, dydx);
     }
-    lane_solve(s, n, err);
+    if (!lane_solve<MIXED>(s, n, err, fp64)) return -1.0;
     lane_map(n, yTemp, [](double y, double d, double e) { return y + d + e; }, y0, dy, err);
     return lane_err_norm(o, n, y0, yTemp, err);
 }
 
 // OptRosenbrock34::Rosenbrock34Solve (OptRosenbrock34.C:281-678), .H:127-158
+template<bool MIXED>
 __device__ __noinline__ double lane_ros34(const DevMech& M, const KOpts& o, const LaneSlot& s, double p, double dx,
-                                          double invdx, CellCounters& cc) {
+                                          double invdx, CellCounters& cc, bool fp64) {
     const int n = M.n;
     const LA<double> y0 = s.v(0), yTemp = s.v(1), k1 = s.v(2), k2 = s.v(3), k3 = s.v(4), k4 = s.v(5);
     const LA<double> err = s.v(8), dydx = s.v(9), dfdx = s.v(10);
@@ -877,13 +974,13 @@ __device__ __noinline__ double lane_ros34(const DevMech& M, const KOpts& o, cons
     const double d1 = 1.0 / 2.0, d2 = -3.0 / 2.0, d3 = 605.0 / 250.0, d4 = 29.0 / 250.0;
     const double invgamma = 1.0 / (1.0 / 2.0);
     const double cdiag = invdx * invgamma;
-    lane_jacobian_and_lu(M, o, s, p, cdiag);
+    lane_jacobian_and_lu<MIXED>(M, o, s, p, cdiag, fp64);
     cc.jac++; cc.lu++; cc.rhs += 2; cc.solves += 4;
 
     const double dxd1 = dx * d1 + 1;
     #pragma unroll 1
     for (int i = 0; i < n; i++) k1[i] = dxd1 * dfdx[i];
-    lane_solve(s, n, k1);
+    if (!lane_solve<MIXED>(s, n, k1, fp64)) return -1.0;
     #pragma unroll 1
     for (int i = 0; i < n; i++) yTemp[i] = fma(a21, k1[i], y0[i]);
     lane_rhs(M, s, p, yTemp, dydx, 1);
@@ -892,7 +989,7 @@ __device__ __noinline__ double lane_ros34(const DevMech& M, const KOpts& o, cons
         #pragma unroll 1
         for (int i = 0; i < n; i++) k2[i] = fma(f1, k1[i], fma(dxd2, dfdx[i], dydx[i]));
     }
-    lane_solve(s, n, k2);
+    if (!lane_solve<MIXED>(s, n, k2, fp64)) return -1.0;
     #pragma unroll 1
     for (int i = 0; i < n; i++) yTemp[i] = fma(a32, k2[i], fma(a31, k1[i], y0[i]));
     lane_rhs(M, s, p, yTemp, dydx, 1);
@@ -901,14 +998,14 @@ __device__ __noinline__ double lane_ros34(const DevMech& M, const KOpts& o, cons
         #pragma unroll 1
         for (int i = 0; i < n; i++) k3[i] = fma(f2, k2[i], fma(f1, k1[i], fma(dxd3, dfdx[i], dydx[i])));
     }
-    lane_solve(s, n, k3);
+    if (!lane_solve<MIXED>(s, n, k3, fp64)) return -1.0;
     {
         const double dxd4 = dx * d4, f1 = c41 * invdx, f2 = c42 * invdx, f3 = c43 * invdx;
         #pragma unroll 1
         for (int i = 0; i < n; i++)
             k4[i] = fma(f3, k3[i], fma(f2, k2[i], fma(f1, k1[i], fma(dxd4, dfdx[i], dydx[i]))));
     }
-    lane_solve(s, n, k4);
+    if (!lane_solve<MIXED>(s, n, k4, fp64)) return -1.0;
     #pragma unroll 1
     for (int i = 0; i < n; i++) {
         yTemp[i] = fma(b4, k4[i], fma(b3, k3[i], fma(b2, k2[i], fma(b1, k1[i], y0[i]))));
@@ -918,8 +1015,9 @@ __device__ __noinline__ double lane_ros34(const DevMech& M, const KOpts& o, cons
 }
 
 // OptRodas23::Rodas23Solve (OptRodas23.C:202-315), constants OptRodas23.H:113-126
+template<bool MIXED>
 __device__ __noinline__ double lane_rodas23(const DevMech& M, const KOpts& o, const LaneSlot& s, double p, double dx,
-                                            double invdx, CellCounters& cc) {
+                                            double invdx, CellCounters& cc, bool fp64) {
     const int n = M.n;
     const LA<double> y0 = s.v(0), yTemp = s.v(1), k1 = s.v(2), k2 = s.v(3), k3 = s.v(4);
     const LA<double> dy = s.v(7), err = s.v(8), dydx = s.v(9), dfdx = s.v(10);
@@ -927,16 +1025,16 @@ __device__ __noinline__ double lane_rodas23(const DevMech& M, const KOpts& o, co
     const double c41 = 1, c42 = -1, c43 = -8.0 / 3.0;
     const double invgamma = 1.0 / (1.0 / 2.0);
     const double cdiag = invdx * invgamma;
-    lane_jacobian_and_lu(M, o, s, p, cdiag);
+    lane_jacobian_and_lu<MIXED>(M, o, s, p, cdiag, fp64);
     cc.jac++; cc.lu++; cc.rhs += 2; cc.solves += 4;
 
     const double dxd1 = dx * d1, dxd2 = dx * d2;
     #pragma unroll 1
     for (int i = 0; i < n; i++) k1[i] = fma(dxd1, dfdx[i], dfdx[i]);
-    lane_solve(s, n, k1);
+    if (!lane_solve<MIXED>(s, n, k1, fp64)) return -1.0;
     #pragma unroll 1
     for (int i = 0; i < n; i++) k2[i] = fma(dxd2, dfdx[i], dfdx[i]) + c21 * k1[i] / dx;
-    lane_solve(s, n, k2);
+    if (!lane_solve<MIXED>(s, n, k2, fp64)) return -1.0;
     #pragma unroll 1
     for (int i = 0; i < n; i++) {
         dy[i] = a31 * k1[i];
@@ -945,7 +1043,7 @@ __device__ __noinline__ double lane_rodas23(const DevMech& M, const KOpts& o, co
     lane_rhs(M, s, p, yTemp, dydx, 1);
     #pragma unroll 1
     for (int i = 0; i < n; i++) k3[i] = dydx[i] + fma(c32, k2[i], c31 * k1[i]) / dx;
-    lane_solve(s, n, k3);
+    if (!lane_solve<MIXED>(s, n, k3, fp64)) return -1.0;
     #pragma unroll 1
     for (int i = 0; i < n; i++) {
         dy[i] = dy[i] + k3[i];
@@ -954,15 +1052,16 @@ __device__ __noinline__ double lane_rodas23(const DevMech& M, const KOpts& o, co
     lane_rhs(M, s, p, yTemp, dydx, 1);
     #pragma unroll 1
     for (int i = 0; i < n; i++) err[i] = dydx[i] + fma(c43, k3[i], fma(c42, k2[i], c41 * k1[i])) / dx;
-    lane_solve(s, n, err);
+    if (!lane_solve<MIXED>(s, n, err, fp64)) return -1.0;
     #pragma unroll 1
     for (int i = 0; i < n; i++) yTemp[i] = y0[i] + dy[i] + err[i];
     return lane_err_norm(o, n, y0, yTemp, err);
 }
 
 // OptRosenbrock23::Rosenbrock23Solve (OptRosenbrock23.C:208-298), constants .H:116-140
+template<bool MIXED>
 __device__ __noinline__ double lane_ros23(const DevMech& M, const KOpts& o, const LaneSlot& s, double p, double dx,
-                                          double invdx, CellCounters& cc) {
+                                          double invdx, CellCounters& cc, bool fp64) {
     const int n = M.n;
     const LA<double> y0 = s.v(0), yTemp = s.v(1), k1 = s.v(2), k2 = s.v(3), k3 = s.v(4);
     const LA<double> err = s.v(8), dydx = s.v(9), dfdx = s.v(10);
@@ -975,22 +1074,22 @@ __device__ __noinline__ double lane_ros23(const DevMech& M, const KOpts& o, cons
     const double d1 = 0.43586652150845899941601945119356, d2 = 0.24291996454816804366592249683314;
     const double d3 = 2.1851380027664058511513169485832;
     const double cdiag = invdx * invgamma;
-    lane_jacobian_and_lu(M, o, s, p, cdiag);
+    lane_jacobian_and_lu<MIXED>(M, o, s, p, cdiag, fp64);
     cc.jac++; cc.lu++; cc.rhs += 1; cc.solves += 3;
 
     const double dxd1 = dx * d1, dxd2 = dx * d2, dxd3 = dx * d3;
     #pragma unroll 1
     for (int i = 0; i < n; i++) k1[i] = fma(dxd1, dfdx[i], dfdx[i]);
-    lane_solve(s, n, k1);
+    if (!lane_solve<MIXED>(s, n, k1, fp64)) return -1.0;
     #pragma unroll 1
     for (int i = 0; i < n; i++) yTemp[i] = fma(a21, k1[i], y0[i]);
     lane_rhs(M, s, p, yTemp, dydx, 1);
     #pragma unroll 1
     for (int i = 0; i < n; i++) k2[i] = fma(dxd2, dfdx[i], dydx[i]) + c21 * k1[i] / dx;
-    lane_solve(s, n, k2);
+    if (!lane_solve<MIXED>(s, n, k2, fp64)) return -1.0;
     #pragma unroll 1
     for (int i = 0; i < n; i++) k3[i] = fma(dxd3, dfdx[i], dydx[i]) + fma(c32, k2[i], c31 * k1[i]) / dx;
-    lane_solve(s, n, k3);
+    if (!lane_solve<MIXED>(s, n, k3, fp64)) return -1.0;
     #pragma unroll 1
     for (int i = 0; i < n; i++) {
         yTemp[i] = fma(b3, k3[i], fma(b2, k2[i], fma(b1, k1[i], y0[i])));
@@ -999,14 +1098,15 @@ __device__ __noinline__ double lane_ros23(const DevMech& M, const KOpts& o, cons
     return lane_err_norm(o, n, y0, yTemp, err);
 }
 
+template<bool MIXED>
 __device__ __forceinline__ double lane_attempt(const DevMech& M, const KOpts& o, const LaneSlot& s, double p,
-                                               double dx, CellCounters& cc) {
+                                               double dx, CellCounters& cc, bool fp64) {
     const double invdx = 1.0 / dx;
     switch (o.solver) {
-        case FCS_SOLVER_ROSENBROCK34: return lane_ros34(M, o, s, p, dx, invdx, cc);
-        case FCS_SOLVER_RODAS23: return lane_rodas23(M, o, s, p, dx, invdx, cc);
-        case FCS_SOLVER_ROSENBROCK23: return lane_ros23(M, o, s, p, dx, invdx, cc);
-        default: return lane_rodas34(M, o, s, p, dx, invdx, cc);
+        case FCS_SOLVER_ROSENBROCK34: return lane_ros34<MIXED>(M, o, s, p, dx, invdx, cc, fp64);
+        case FCS_SOLVER_RODAS23: return lane_rodas23<MIXED>(M, o, s, p, dx, invdx, cc, fp64);
+        case FCS_SOLVER_ROSENBROCK23: return lane_ros23<MIXED>(M, o, s, p, dx, invdx, cc, fp64);
+        default: return lane_rodas34<MIXED>(M, o, s, p, dx, invdx, cc, fp64);
     }
 }
 
@@ -1023,6 +1123,8 @@ struct LaneCtl {
     int att;          // attempts on this cell
     int nStep, rejects;
     bool last, retry;
+    bool redo;        // repeat the last attempt with the same step (mixed precision, now in FP64)
+    bool fp64;        // this attempt in FP64: the mixed attempt's refinement check failed
 };
 
 template<class MT>
@@ -1030,6 +1132,7 @@ __global__ void __launch_bounds__(128, 4)
 lane_integrate_kernel(const DevMech M, const KOpts o, const LaneLayout L, CellIO io, WorkQueue q,
                       double* __restrict__ ws) {
     const unsigned FULL = 0xffffffffu;
+    constexpr bool kMixed = sizeof(MT) == 4;
     const int lane = threadIdx.x & 31;
     const long long gwarp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const LaneSlot s = make_lane_slot(ws + (size_t)gwarp * L.words * kLanes, L);
@@ -1076,6 +1179,8 @@ lane_integrate_kernel(const DevMech M, const KOpts o, const LaneLayout L, CellIO
                     k.nStep = 0;
                     k.att = 0;
                     k.last = false;
+                    k.redo = false;
+                    k.fp64 = false;
                     k.retry = false;
                 }
             }
@@ -1087,7 +1192,7 @@ lane_integrate_kernel(const DevMech M, const KOpts o, const LaneLayout L, CellIO
                 st = FCS_CELL_OK;  // nothing to integrate (transientSolve.H's loop does not run)
             } else {
                 // 2. the step size of this attempt
-                if (!k.retry) {
+                if (!k.retry && !k.redo) {
                     k.dxTry0 = k.dxTry;
                     if ((k.x + k.dxTry - k.deltaT) * (k.x + k.dxTry - 0.0) > 0) {
                         k.last = true;
@@ -1097,31 +1202,41 @@ lane_integrate_kernel(const DevMech M, const KOpts o, const LaneLayout L, CellIO
                     k.rejects = 0;
                 }
                 // 3. one attempt (the same code on every lane)
-                const double Err = lane_attempt(M, o, s, k.p, k.dx, cc);
-                cc.attempts++;
-                k.att++;
-                // 4. the controller
-                if (Err > 1) {
-                    if (++k.rejects > o.maxRejects) {
-                        st = FCS_CELL_DT_UNDERFLOW;
-                    } else {
-                        k.dx *= fmax(SAFE * pow(Err, -ALPHA_DEC), MIN_SCALE);
-                        k.retry = true;
-                    }
-                } else if (!(Err == Err)) {
-                    st = FCS_CELL_NONFINITE;
+                k.redo = false;
+                const double Err = lane_attempt<kMixed>(M, o, s, k.p, k.dx, cc, k.fp64);
+                if (kMixed && Err == -1.0) {
+                    // the FP32 factors failed the refinement check: the same
+                    // attempt again in FP64 (counted once, as in the cell groups)
+                    cc.fallbacks++;
+                    k.fp64 = true;
+                    k.redo = true;
                 } else {
-                    cc.accepted++;
-                    k.retry = false;
-                    k.x += k.dx;
-                    lane_map(n, y, [](double v) { return v; }, yTemp);
-                    k.dxTry = (Err > ratio) ? fmin(fmax(SAFE * pow(Err, -ALPHA_INC), MIN_SCALE), MAX_SCALE) * k.dx
-                                            : safeMaxScale * k.dx;
-                    if ((k.x - k.deltaT) * (k.deltaT - 0.0) >= 0) {
-                        if (k.nStep > 0 && k.last) k.dxTry = k.dxTry0;
-                        st = FCS_CELL_OK;
-                    } else if (++k.nStep >= o.maxSteps) {
-                        st = FCS_CELL_MAX_STEPS;
+                    k.fp64 = false;
+                    cc.attempts++;
+                    k.att++;
+                    // 4. the controller
+                    if (Err > 1) {
+                        if (++k.rejects > o.maxRejects) {
+                            st = FCS_CELL_DT_UNDERFLOW;
+                        } else {
+                            k.dx *= fmax(SAFE * pow(Err, -ALPHA_DEC), MIN_SCALE);
+                            k.retry = true;
+                        }
+                    } else if (!(Err == Err)) {
+                        st = FCS_CELL_NONFINITE;
+                    } else {
+                        cc.accepted++;
+                        k.retry = false;
+                        k.x += k.dx;
+                        lane_map(n, y, [](double v) { return v; }, yTemp);
+                        k.dxTry = (Err > ratio) ? fmin(fmax(SAFE * pow(Err, -ALPHA_INC), MIN_SCALE), MAX_SCALE) * k.dx
+                                                : safeMaxScale * k.dx;
+                        if ((k.x - k.deltaT) * (k.deltaT - 0.0) >= 0) {
+                            if (k.nStep > 0 && k.last) k.dxTry = k.dxTry0;
+                            st = FCS_CELL_OK;
+                        } else if (++k.nStep >= o.maxSteps) {
+                            st = FCS_CELL_MAX_STEPS;
+                        }
                     }
                 }
             }

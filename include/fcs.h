@@ -94,7 +94,7 @@ enum { FCS_JACOBIAN_EXACT = 0, FCS_JACOBIAN_FAST = 1 };
 enum { FCS_PRECISION_FP64 = 0, FCS_PRECISION_MIXED = 1 };
 /* Cell-to-thread mapping: AUTO lets the autotuner choose.  LANE: one thread
  * per cell, the cells' working sets in a global-memory workspace interleaved
- * across the lanes of a warp (Rosenbrock-family solvers in FP64); the others:
+ * across the lanes of a warp (Rosenbrock-family solvers, FP64 or mixed); the others:
  * a group of 32..256 threads per cell with its working set in shared memory
  * (or in global memory when it does not fit). */
 enum { FCS_MAPPING_AUTO = 0, FCS_MAPPING_LANE = 1, FCS_MAPPING_WARP = 32, FCS_MAPPING_BLOCK64 = 64,

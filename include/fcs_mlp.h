@@ -106,8 +106,8 @@ fcs_status fcs_mlp_load(fcs_mlp** out, int device, const char* path);
  * surrogate error seen on them is reported.
  */
 typedef struct fcs_gate_options {
-    double T_rel;           /* default 2e-4 */
-    double Y_abs;           /* default 2e-7 */
+    double T_rel;           /* default 1e-3 (the method's target accuracy in T) */
+    double Y_abs;           /* default 1e-6 (the method's target accuracy in Y_i) */
     double element_abs;     /* default 1e-6 */
     double audit_fraction;  /* default 0.02 */
     int32_t seed_substep;   /* default 1 */

@@ -87,16 +87,24 @@ def test_lane_matches_group_mapping(built, wname, n):
     for k in ("cells_integrated", "cells_skipped", "cells_failed"):
         assert b["stats"][k] == a["stats"][k], k
     assert abs(b["stats"]["attempts"] - a["stats"]["attempts"]) <= 0.002 * a["stats"]["attempts"] + 4
-    np.testing.assert_allclose(b["T"], a["T"], rtol=1e-8)
-    np.testing.assert_allclose(b["Y"], a["Y"], atol=1e-9)
-    # RR = (Y1 - Y0) rho0 / dt: the Y tolerance carried over
-    np.testing.assert_allclose(b["RR"], a["RR"], atol=1e-9 * c.rho0.max() / w.dt)
+    # the mixture sums run in a different order: rounding-level differences,
+    # grown through ~250 stiff steps.  Most cells take the same steps and
+    # agree to the golden-fixture tolerances; a cell whose rounding tips one
+    # accept/reject decision takes other steps and lands elsewhere within the
+    # integration tolerance (relTol 1e-4).
+    eT = np.abs(b["T"] - a["T"]) / a["T"]
+    eY = np.abs(b["Y"] - a["Y"]).max(axis=0)
+    close = (eT <= 1e-7) & (eY <= 1e-8)
+    assert close.mean() >= 0.99, close.mean()
+    assert eT.max() <= 1e-4 and eY.max() <= 1e-5, (eT.max(), eY.max())
+    eR = np.abs(b["RR"] - a["RR"]).max(axis=0) * w.dt / c.rho0  # RR back in units of Y
+    assert eR.max() <= 1e-5
     assert b["deltaTMin"] == pytest.approx(a["deltaTMin"], rel=1e-6)
 
 
 def test_lane_failure_statuses_and_lts(built):
-    """maxSteps and NaN pressure fail only their own cells (the others are
-    integrated, as with the group mapping); per-cell delta_t (LTS)."""
+    """maxSteps and NaN pressure fail only their own cells, as with the group
+    mapping; the other cells are still integrated; per-cell delta_t (LTS)."""
     import oracle
     w, mech, flat, c = _setup("ignition_10s", 96)
     c.p[5] = np.nan
@@ -104,10 +112,13 @@ def test_lane_failure_statuses_and_lts(built):
     out = ctx.integrate(c, w.dt)
     grp = _ctx(flat, abs_tol=w.abs_tol, rel_tol=w.rel_tol, mapping=64, max_steps=3).integrate(c, w.dt)
     np.testing.assert_array_equal(out["status"], grp["status"])
-    assert out["status"][5] == 2 and (out["status"] == 1).sum() > 10 and (out["status"] == 0).sum() > 10
-    ok = out["status"] == 0
-    np.testing.assert_allclose(out["T"][ok], grp["T"][ok], rtol=1e-10)
-    np.testing.assert_array_equal(out["subDt"][~ok], grp["subDt"][~ok])
+    assert out["status"][5] == 2 and (out["status"] == 1).sum() > 10
+    np.testing.assert_array_equal(out["subDt"], grp["subDt"])   # failed cells keep their sub-step
+    ctx.set_options(abs_tol=w.abs_tol, rel_tol=w.rel_tol, mapping=LANE)
+    out = ctx.integrate(c, w.dt)
+    ref = oracle.Port(flat).integrate(c.subset(np.arange(5)), w.dt, abs_tol=w.abs_tol, rel_tol=w.rel_tol)
+    assert out["status"][5] == 2 and (np.delete(out["status"], 5) == 0).all()
+    np.testing.assert_allclose(out["T"][:5], ref["T"], rtol=1e-9)
     # LTS: per-cell delta_t
     w, mech, flat, c = _setup("ignition_10s", 64)
     dtc = np.geomspace(1e-7, 2e-5, c.n)
@@ -156,3 +167,31 @@ def test_lane_refused_where_it_does_not_apply(built):
     ctx.set_options(mapping=LANE)
     f = ctx.rhs(c.p, c.T, c.Y)  # the per-cell evaluations use cell groups
     assert np.isfinite(f).all()
+
+
+@pytest.mark.parametrize("fixture_name,wname", [("counterflow_53s_tight", "counterflow_53s"),
+                                                ("large_200s_tight", "large_200s")])
+@pytest.mark.parametrize("solver", ["OptRodas34", "OptRosenbrock34"])
+def test_lane_mixed_precision_accuracy(built, fixture_name, wname, solver):
+    """The lane mapping in mixed precision (FP32 factors of the equilibrated
+    iteration matrix, one FP64-residual refinement per solve, an attempt
+    whose correction is not small redone in FP64) against the reference's
+    tight run: no cell lost, within 2x of the FP64 method's own error plus a
+    floor, <= 1e-3 relative in T."""
+    g = np.load(os.path.join(GOLDEN, fixture_name + ".npz"))
+    w = fcs.WORKLOADS[wname]
+    flat, c = fixture.load(g)
+    ctx = _ctx(flat, solver=solver, abs_tol=w.abs_tol, rel_tol=w.rel_tol, precision="fp64", mapping=LANE)
+    f64 = ctx.integrate(c, w.dt)
+    ctx.set_options(solver=solver, abs_tol=w.abs_tol, rel_tol=w.rel_tol, precision="mixed", mapping=LANE)
+    mix = ctx.integrate(c, w.dt)
+    assert mix["stats"]["mapping"] == LANE
+    assert (mix["status"] == 0).all() and (f64["status"] == 0).all()
+    eT64 = np.max(np.abs(f64["T"] - g["T"]) / g["T"])
+    eY64 = np.max(np.abs(f64["Y"] - g["Y"]))
+    eT = np.max(np.abs(mix["T"] - g["T"]) / g["T"])
+    eY = np.max(np.abs(mix["Y"] - g["Y"]))
+    assert eT <= 2 * eT64 + 1e-5 and eT <= 1e-3, (eT, eT64)
+    assert eY <= 2 * eY64 + 1e-6, (eY, eY64)
+    # the FP64 redo is the exception, not the rule
+    assert mix["stats"]["fp64_fallbacks"] <= 0.25 * mix["stats"]["attempts"]
