@@ -702,34 +702,35 @@ __device__ __noinline__ void lane_lu(LA<T> A, int n, LA<int> piv, LA<double> inv
                 if (two) rk[j + 1] = r1;
             }
         }
-        // (c) the trailing block: A[i][j] -= sum over the panel's m, in order;
-        // two columns per step, all ten loads first
-        const LA<T> u0 = A + k0 * n, u1 = A + (k0 + 1) * n;
-        const LA<T> u2 = A + (k0 + (size > 2 ? 2 : 1)) * n, u3 = A + (k0 + (size > 3 ? 3 : 1)) * n;
+        // (c) the trailing block: A[i][j] -= sum over the panel's m, in order
+        // (here size == 4: the remainder panel is the last one).  Four columns
+        // at a time: the panel's U entries of those columns stay in registers
+        // while the rows stream past, 8 loads per 16 multiply-adds.
         #pragma unroll 1
-        for (int i = k1; i < n; i++) {
-            LA<T> ri = A + i * n;
-            const T l0 = ri[k0], l1 = ri[k0 + 1];
-            const T l2 = size > 2 ? ri[k0 + 2] : T(0), l3 = size > 3 ? ri[k0 + 3] : T(0);
-            int j = k1;
-            for (; j + 2 <= n; j += 2) {
-                const T a0 = ri[j], a1 = ri[j + 1];
-                const T p0 = u0[j], p1 = u0[j + 1], q0 = u1[j], q1 = u1[j + 1];
-                const T s0 = u2[j], s1 = u2[j + 1], t0 = u3[j], t1 = u3[j + 1];
-                T r0 = fma(-l0, p0, a0), r1 = fma(-l0, p1, a1);
-                r0 = fma(-l1, q0, r0); r1 = fma(-l1, q1, r1);
-                if (size > 2) { r0 = fma(-l2, s0, r0); r1 = fma(-l2, s1, r1); }
-                if (size > 3) { r0 = fma(-l3, t0, r0); r1 = fma(-l3, t1, r1); }
-                ri[j] = r0;
-                ri[j + 1] = r1;
+        for (int j = k1; j < n; j += 4) {
+            const int nj = n - j;  // >= 1; the last chunk holds n % 4 columns
+            T u[4][4];
+            #pragma unroll
+            for (int m = 0; m < 4; m++) {
+                const LA<T> um = A + (k0 + m) * n + j;
+                #pragma unroll
+                for (int c = 0; c < 4; c++) u[m][c] = c < nj ? um[c] : T(0);
             }
-            if (j < n) {
-                T a = ri[j];
-                a = fma(-l0, u0[j], a);
-                a = fma(-l1, u1[j], a);
-                if (size > 2) a = fma(-l2, u2[j], a);
-                if (size > 3) a = fma(-l3, u3[j], a);
-                ri[j] = a;
+            #pragma unroll 1
+            for (int i = k1; i < n; i++) {
+                const LA<T> ri = A + i * n;
+                T l[4], a[4];
+                #pragma unroll
+                for (int m = 0; m < 4; m++) l[m] = ri[k0 + m];
+                #pragma unroll
+                for (int c = 0; c < 4; c++) a[c] = c < nj ? ri[j + c] : T(0);
+                #pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    T r = a[c];
+                    #pragma unroll
+                    for (int m = 0; m < 4; m++) r = fma(-l[m], u[m][c], r);
+                    if (c < nj) ri[j + c] = r;
+                }
             }
         }
         k0 = k1;
@@ -747,16 +748,65 @@ __device__ __noinline__ void lane_lu_solve(const LA<MT> A, int n, const LA<int> 
         const int p = piv[j];
         if (p != j) { const VT t = b[j]; b[j] = b[p]; b[p] = t; }
     }
+    // Both sweeps take four rows at a time: b[j] is loaded once for the four
+    // rows, each row still sums its terms in the order of the row-by-row sweep
+    // (the terms of the four rows' own triangle last, in that order).
+    int i = 1;
     #pragma unroll 1
-    for (int i = 1; i < n; i++) {
+    for (; i + 4 <= n; i += 4) {
+        const LA<MT> r0 = A + i * n, r1 = r0 + n, r2 = r1 + n, r3 = r2 + n;
+        VT a0 = b[i], a1 = b[i + 1], a2 = b[i + 2], a3 = b[i + 3];
+        #pragma unroll 4
+        for (int j = 0; j < i; j++) {
+            const VT bj = b[j];
+            a0 = fma(-VT(r0[j]), bj, a0);
+            a1 = fma(-VT(r1[j]), bj, a1);
+            a2 = fma(-VT(r2[j]), bj, a2);
+            a3 = fma(-VT(r3[j]), bj, a3);
+        }
+        a1 = fma(-VT(r1[i]), a0, a1);
+        a2 = fma(-VT(r2[i]), a0, a2);
+        a3 = fma(-VT(r3[i]), a0, a3);
+        a2 = fma(-VT(r2[i + 1]), a1, a2);
+        a3 = fma(-VT(r3[i + 1]), a1, a3);
+        a3 = fma(-VT(r3[i + 2]), a2, a3);
+        b[i] = a0; b[i + 1] = a1; b[i + 2] = a2; b[i + 3] = a3;
+    }
+    #pragma unroll 1
+    for (; i < n; i++) {
         const LA<MT> ri = A + i * n;
         VT acc = b[i];
         #pragma unroll 8
         for (int j = 0; j < i; j++) acc = fma(-VT(ri[j]), b[j], acc);
         b[i] = acc;
     }
+    i = n - 1;
     #pragma unroll 1
-    for (int i = n - 1; i >= 0; i--) {
+    for (; i >= 3; i -= 4) {
+        const LA<MT> r0 = A + i * n, r1 = A + (i - 1) * n, r2 = A + (i - 2) * n, r3 = A + (i - 3) * n;
+        VT a0 = b[i], a1 = b[i - 1], a2 = b[i - 2], a3 = b[i - 3];
+        #pragma unroll 4
+        for (int j = n - 1; j > i; j--) {
+            const VT bj = b[j];
+            a0 = fma(-VT(r0[j]), bj, a0);
+            a1 = fma(-VT(r1[j]), bj, a1);
+            a2 = fma(-VT(r2[j]), bj, a2);
+            a3 = fma(-VT(r3[j]), bj, a3);
+        }
+        a0 = a0 * VT(invD[i]);
+        a1 = fma(-VT(r1[i]), a0, a1);
+        a2 = fma(-VT(r2[i]), a0, a2);
+        a3 = fma(-VT(r3[i]), a0, a3);
+        a1 = a1 * VT(invD[i - 1]);
+        a2 = fma(-VT(r2[i - 1]), a1, a2);
+        a3 = fma(-VT(r3[i - 1]), a1, a3);
+        a2 = a2 * VT(invD[i - 2]);
+        a3 = fma(-VT(r3[i - 2]), a2, a3);
+        a3 = a3 * VT(invD[i - 3]);
+        b[i] = a0; b[i - 1] = a1; b[i - 2] = a2; b[i - 3] = a3;
+    }
+    #pragma unroll 1
+    for (; i >= 0; i--) {
         const LA<MT> ri = A + i * n;
         VT acc = b[i];
         #pragma unroll 8
@@ -826,8 +876,27 @@ __device__ __noinline__ bool lane_solve_mixed(const LaneSlot& s, int n, LA<doubl
     lane_lu_solve<float, float>(s.LU32, n, s.piv, s.invD, x32);
     #pragma unroll 4
     for (int i = 0; i < n; i++) tmp[i] = double(x32[i]) * s.dc[i];
+    // the FP64 residual, four rows at a time (tmp[j] loaded once for them)
+    int i = 0;
     #pragma unroll 1
-    for (int i = 0; i < n; i++) {
+    for (; i + 4 <= n; i += 4) {
+        const LA<double> A0 = s.A + i * n, A1 = A0 + n, A2 = A1 + n, A3 = A2 + n;
+        double r0 = b[i], r1 = b[i + 1], r2 = b[i + 2], r3 = b[i + 3];
+        #pragma unroll 4
+        for (int j = 0; j < n; j++) {
+            const double t = tmp[j];
+            r0 = fma(-A0[j], t, r0);
+            r1 = fma(-A1[j], t, r1);
+            r2 = fma(-A2[j], t, r2);
+            r3 = fma(-A3[j], t, r3);
+        }
+        r32[i] = float(r0 * s.dr[i]);
+        r32[i + 1] = float(r1 * s.dr[i + 1]);
+        r32[i + 2] = float(r2 * s.dr[i + 2]);
+        r32[i + 3] = float(r3 * s.dr[i + 3]);
+    }
+    #pragma unroll 1
+    for (; i < n; i++) {
         const LA<double> Ai = s.A + i * n;
         double r = b[i];
         #pragma unroll 8
