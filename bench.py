@@ -70,6 +70,8 @@ def parse():
                          "mlp: only the ensemble forward on the tensor cores (untrained weights)")
     ap.add_argument("--train-samples", type=int, default=65536,
                     help="cells integrated by the plain method to train the surrogate (before timing)")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="launch the plain method's step without a CUDA graph (for profilers)")
     ap.add_argument("--accuracy-cells", type=int, default=256,
                     help="cells checked against a tight-tolerance run (0: skip)")
     return ap.parse_args()
@@ -472,10 +474,10 @@ def main():
     # the first call autotunes the cell-to-thread mapping (outside the graph)
     step_plain(graph=False)
     for _ in range(args.warmup):
-        step_plain()
+        step_plain(graph=not args.no_graph)
     peak64 = _lib.fp64_peak_tflops(local)
     with ClockSampler(local) as clk:
-        t_step, outs = timed(step_plain)
+        t_step, outs = timed(lambda: step_plain(graph=not args.no_graph))
     T_plain, Y_plain = T.cpu().numpy(), Y.cpu().numpy()
     value = ws * n / (t_step * 1e-3)
     s0 = outs[-1][1]
@@ -559,14 +561,20 @@ def main():
     attempts = s0["attempts"]
     k_ms = statistics.mean(kms)
     achieved = f64 * attempts / (k_ms * 1e-3) / 1e12
+    # DRAM traffic of one launch from an ncu capture of the same kernel on a
+    # smaller case, scaled by attempts (the workspace traffic of the lane
+    # mapping) or by cells (the state I/O of the cell groups)
     traffic = None
     tj = os.path.join(HERE, "profiles", "integrate_traffic.json")
     if os.path.exists(tj):
         with open(tj) as f:
             tr = json.load(f)
-        key = f"{args.workload}/{args.solver}/{args.precision}"
-        if key in tr:
-            traffic = tr[key]["bytes_per_cell"] * n
+        mapping = "lane" if s0["mapping"] == 1 else f"g{s0['mapping']}"
+        rec = tr.get(f"{args.workload}/{args.solver}/{args.precision}/{mapping}")
+        if rec and "bytes_per_attempt" in rec:
+            traffic = rec["bytes_per_attempt"] * s0["attempts"]
+        elif rec:
+            traffic = rec["bytes_per_cell"] * n
     if rank != 0:
         return
     line = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,

@@ -26,12 +26,6 @@ __device__ __forceinline__ int step_bin(double deltaT, double sub) {
     return b < 0 ? 0 : (b >= 32 ? 31 : b);
 }
 
-// eight bins per octave of the previous integration's attempts (8 .. 2048)
-__device__ __forceinline__ int attempt_bin(int attempts) {
-    const int b = (int)floorf(8.f * log2f((float)(attempts > 1 ? attempts : 1))) - 24;
-    return b < 0 ? 0 : (b >= kQueueBins ? kQueueBins - 1 : b);
-}
-
 __global__ void classify_bin_kernel(CellIO io, int ns, double Treact, int* bin, int* counters) {
     __shared__ int hist[kQueueBins];
     for (int b = threadIdx.x; b < kQueueBins; b += blockDim.x) hist[b] = 0;

@@ -87,6 +87,8 @@ struct GateArgs {
     double* RR;
     int* status;
     int* bin;
+    const int* attempts;           // per cell: attempts of the previous integration of this batch
+    int attemptsValid;             // attempts[] is valid: bins by it, as the plain method's queue
     int* counters;
     int* auditCell;
     double* auditPred;
@@ -200,15 +202,22 @@ __global__ void __launch_bounds__(256) gate_kernel(const GateArgs a) {
         atomicAdd(&a.gstats[GS_FALLBACK], 1ull);
     }
     if (lane == 0) {
-        // predicted step count -> bin (0: cheapest)
+        // the cell's cost -> bin (0: cheapest): its attempts in the previous
+        // integration of this batch when the context holds them, else the
+        // step count predicted from its sub-step
         double sub = a.sub[c];
         if (a.seedSub && isfinite(subP) && subP > 0) {
             sub = fmin(fmax(subP, 1e-14), a.dt);
             a.sub[c] = sub;
         }
-        const double steps = a.dt / fmax(sub, 1e-300);
-        int b = steps > 1 ? (int)log2(steps) : 0;
-        b = b < 0 ? 0 : (b >= kQueueBins ? kQueueBins - 1 : b);
+        int b;
+        if (a.attemptsValid) {
+            b = attempt_bin(a.attempts[c]);
+        } else {
+            const double steps = a.dt / fmax(sub, 1e-300);
+            b = steps > 1 ? (int)log2(steps) : 0;
+            b = b < 0 ? 0 : (b >= kQueueBins ? kQueueBins - 1 : b);
+        }
         a.bin[c] = b;
         atomicAdd(&a.counters[QC_BINS + b], 1);
     }
@@ -343,6 +352,12 @@ extern "C" fcs_status fcs_integrate_gated(fcs_ctx* ctx, int64_t nc, double dt, c
     CK(g->auditPred.ensure((size_t)std::max(auditCap, 1) * (ns + 1)));
     io.stats = ctx->bStats.p;
     io.dtMinBits = ctx->bMin.p;
+    // per-cell attempts of the previous integration of a batch of this size
+    // (plain or gated) order the fallback queue, as in the plain method
+    if (ctx->bAtt.n < (size_t)std::max<int64_t>(nc, 1)) ctx->attN = 0;
+    CK(ctx->bAtt.ensure(std::max<int64_t>(nc, 1)));
+    io.attempts = ctx->bAtt.p;
+    const int attValid = ctx->attN == nc ? 1 : 0;
     CK(cudaMemsetAsync(ctx->bStats.p, 0, ST_COUNT * sizeof(long long), st));
     CK(cudaMemsetAsync(ctx->bMin.p, 0x7f, sizeof(unsigned long long), st));
     CK(cudaMemsetAsync(ctx->bHead.p, 0, 2 * sizeof(int), st));
@@ -381,6 +396,7 @@ extern "C" fcs_status fcs_integrate_gated(fcs_ctx* ctx, int64_t nc, double dt, c
         a.seedSub = g->opt.seed_substep; a.auditCap = auditCap;
         a.y = g->y.p; a.factor = g->factor.p; a.rho0 = io.rho0; a.T = io.T; a.Y = io.Y; a.sub = io.subDt;
         a.RR = io.RR; a.status = io.status; a.bin = g->bin.p; a.counters = g->counters.p;
+        a.attempts = io.attempts; a.attemptsValid = attValid;
         a.auditCell = g->auditCell.p; a.auditPred = g->auditPred.p; a.gstats = g->gstats.p;
         a.dtMinBits = ctx->bMin.p;
         const long long wTot = nc * 32;
@@ -396,6 +412,9 @@ extern "C" fcs_status fcs_integrate_gated(fcs_ctx* ctx, int64_t nc, double dt, c
         audit_kernel<<<(int)((aTot + 255) / 256), 256, 0, st>>>(ns, nc, auditCap, g->counters.p, g->auditCell.p,
                                                                  g->auditPred.p, io.T, io.Y, g->gstats.p);
         CK(cudaGetLastError());
+        // the integrator recorded the attempts of the cells it ran; accepted
+        // cells keep their earlier counts
+        ctx->attN = nc;
     } else {
         CK(cudaEventRecord(ctx->ev0, st));
         CK(cudaEventRecord(ctx->ev1, st));

@@ -40,6 +40,15 @@ constexpr int kQueueBins = 64;
 enum { QC_HEAD = 0, QC_LEN = 1, QC_BINS = 2, QC_FILL = QC_BINS + kQueueBins, QC_AUX = QC_FILL + kQueueBins,
        QC_COUNT };
 
+#ifdef __CUDACC__
+// Queue bin of a cell whose previous integration took `attempts` attempted
+// steps: eight bins per octave from 8 to 2048 attempts (0: cheapest).
+__device__ __forceinline__ int attempt_bin(int attempts) {
+    const int b = (int)floorf(8.f * log2f((float)(attempts > 1 ? attempts : 1))) - 24;
+    return b < 0 ? 0 : (b >= kQueueBins ? kQueueBins - 1 : b);
+}
+#endif
+
 struct LaunchCfg {
     int group;                 // threads per cell: 32, 64, 128, 256, or 1 (lane per cell)
     int block;                 // threads per block
