@@ -668,8 +668,22 @@ __device__ __noinline__ void lane_lu(LA<T> A, int n, LA<int> piv, LA<double> inv
             const T u2 = k + 2 < k1 ? A[k * n + k + 2] : T(0);
             const T u3 = k + 3 < k1 ? A[k * n + k + 3] : T(0);
             const int w = k1 - k - 1;  // remaining panel columns: 0..3
+            // two rows per step, both rows' loads issued before any store
+            int i = k + 1;
             #pragma unroll 1
-            for (int i = k + 1; i < n; i++) {
+            for (; i + 2 <= n; i += 2) {
+                LA<T> ri = A + i * n, rj = ri + n;
+                const T a = ri[k], c = rj[k];
+                const T b1 = w > 0 ? ri[k + 1] : T(0), b2 = w > 1 ? ri[k + 2] : T(0), b3 = w > 2 ? ri[k + 3] : T(0);
+                const T d1 = w > 0 ? rj[k + 1] : T(0), d2 = w > 1 ? rj[k + 2] : T(0), d3 = w > 2 ? rj[k + 3] : T(0);
+                const T l = a * rinv, m = c * rinv;
+                ri[k] = l;
+                rj[k] = m;
+                if (w > 0) { ri[k + 1] = fma(-l, u1, b1); rj[k + 1] = fma(-m, u1, d1); }
+                if (w > 1) { ri[k + 2] = fma(-l, u2, b2); rj[k + 2] = fma(-m, u2, d2); }
+                if (w > 2) { ri[k + 3] = fma(-l, u3, b3); rj[k + 3] = fma(-m, u3, d3); }
+            }
+            if (i < n) {
                 LA<T> ri = A + i * n;
                 const T a = ri[k];
                 const T b1 = w > 0 ? ri[k + 1] : T(0), b2 = w > 1 ? ri[k + 2] : T(0), b3 = w > 2 ? ri[k + 3] : T(0);
@@ -716,8 +730,35 @@ __device__ __noinline__ void lane_lu(LA<T> A, int n, LA<int> piv, LA<double> inv
                 #pragma unroll
                 for (int c = 0; c < 4; c++) u[m][c] = c < nj ? um[c] : T(0);
             }
+            // two rows per step: 16 loads in flight before the stores
+            int i = k1;
             #pragma unroll 1
-            for (int i = k1; i < n; i++) {
+            for (; i + 2 <= n; i += 2) {
+                const LA<T> r0 = A + i * n, r1 = r0 + n;
+                T l[2][4], a[2][4];
+                #pragma unroll
+                for (int m = 0; m < 4; m++) { l[0][m] = r0[k0 + m]; l[1][m] = r1[k0 + m]; }
+                #pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    a[0][c] = c < nj ? r0[j + c] : T(0);
+                    a[1][c] = c < nj ? r1[j + c] : T(0);
+                }
+                #pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    #pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        T r = a[h][c];
+                        #pragma unroll
+                        for (int m = 0; m < 4; m++) r = fma(-l[h][m], u[m][c], r);
+                        a[h][c] = r;
+                    }
+                }
+                #pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    if (c < nj) { r0[j + c] = a[0][c]; r1[j + c] = a[1][c]; }
+                }
+            }
+            if (i < n) {
                 const LA<T> ri = A + i * n;
                 T l[4], a[4];
                 #pragma unroll
@@ -1196,8 +1237,10 @@ struct LaneCtl {
     bool fp64;        // this attempt in FP64: the mixed attempt's refinement check failed
 };
 
+// Three resident blocks of 128 threads per SM (the launch shape's default):
+// up to 168 registers per thread, so the RHS and Jacobian run without spills.
 template<class MT>
-__global__ void __launch_bounds__(128, 4)
+__global__ void __launch_bounds__(128, 3)
 lane_integrate_kernel(const DevMech M, const KOpts o, const LaneLayout L, CellIO io, WorkQueue q,
                       double* __restrict__ ws) {
     const unsigned FULL = 0xffffffffu;
