@@ -128,6 +128,20 @@ def flops_per_attempt(ns, nr, ntb, nplog, solver, precision):
     return fp64, fp32, n_rhs * (ns + nr + 2) + (ns + nr + 2)
 
 
+def launch_traffic(records, workload, solver, precision, mapping, attempts, cells):
+    """DRAM bytes of one integrator launch from an ncu capture of the same
+    kernel and mapping on a smaller case (`records`: profiles/integrate_traffic.json),
+    scaled by attempts (the lane mapping's workspace traffic) or by cells (the
+    cell groups' state I/O and stack write-back); None without a record."""
+    name = "lane" if mapping == 1 else f"g{mapping}"
+    rec = records.get(f"{workload}/{solver}/{precision}/{name}")
+    if not rec:
+        return None
+    if "bytes_per_attempt" in rec:
+        return rec["bytes_per_attempt"] * attempts
+    return rec["bytes_per_cell"] * cells
+
+
 class ClockSampler:
     """nvidia-smi samples during the timed region."""
 
@@ -561,20 +575,12 @@ def main():
     attempts = s0["attempts"]
     k_ms = statistics.mean(kms)
     achieved = f64 * attempts / (k_ms * 1e-3) / 1e12
-    # DRAM traffic of one launch from an ncu capture of the same kernel on a
-    # smaller case, scaled by attempts (the workspace traffic of the lane
-    # mapping) or by cells (the state I/O of the cell groups)
     traffic = None
     tj = os.path.join(HERE, "profiles", "integrate_traffic.json")
     if os.path.exists(tj):
         with open(tj) as f:
-            tr = json.load(f)
-        mapping = "lane" if s0["mapping"] == 1 else f"g{s0['mapping']}"
-        rec = tr.get(f"{args.workload}/{args.solver}/{args.precision}/{mapping}")
-        if rec and "bytes_per_attempt" in rec:
-            traffic = rec["bytes_per_attempt"] * s0["attempts"]
-        elif rec:
-            traffic = rec["bytes_per_cell"] * n
+            traffic = launch_traffic(json.load(f), args.workload, args.solver, args.precision, s0["mapping"],
+                                     s0["attempts"], n)
     if rank != 0:
         return
     line = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
