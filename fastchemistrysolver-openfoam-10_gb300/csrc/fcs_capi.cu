@@ -387,10 +387,10 @@ KOpts fcs::kopts(const fcs_options& o) {
     return k;
 }
 
-// Lane per cell (FCS_MAPPING_LANE): blocks of 128 threads, as many per SM
-// as the registers allow (at most 4), a global-memory workspace of
-// make_lane_layout(...).words doubles per thread.  Rosenbrock-family solvers,
-// FP64 or mixed precision.
+// Lane per cell (FCS_MAPPING_LANE): blocks of 128 threads, three per SM
+// (the kernel is compiled for three: 168 registers per thread), a
+// global-memory workspace of make_lane_layout(...).words doubles per thread.
+// Rosenbrock-family solvers, FP64 or mixed precision.
 static bool make_lane_shape(fcs_ctx* ctx, bool integrate, Shape& sh) {
     const fcs_options& o = ctx->opt;
     const bool mixed = o.precision == FCS_PRECISION_MIXED;
