@@ -16,6 +16,7 @@
 #include <fstream>
 #include <map>
 #include <memory>
+#include <new>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -45,6 +46,7 @@ struct Lexer {
     std::string s;
     size_t i = 0;
     std::string dir;
+    std::string bad;  // an unterminated comment or string (the file cannot be read as OpenFOAM reads it)
     explicit Lexer(std::string text, std::string d) : s(std::move(text)), dir(std::move(d)) {}
     void skip() {
         for (;;) {
@@ -54,6 +56,7 @@ struct Lexer {
             } else if (i + 1 < s.size() && s[i] == '/' && s[i + 1] == '*') {
                 i += 2;
                 while (i + 1 < s.size() && !(s[i] == '*' && s[i + 1] == '/')) i++;
+                if (i + 1 >= s.size()) bad = "unterminated /* comment";
                 i += 2;
             } else {
                 return;
@@ -76,6 +79,7 @@ struct Lexer {
             size_t j = i + 1;
             std::string out;
             while (j < s.size() && s[j] != '"') out += s[j++];
+            if (j >= s.size()) bad = "unterminated string";
             i = j + 1;
             if (quoted) *quoted = true;
             return out;
@@ -92,6 +96,7 @@ struct Lexer {
             if (s[j] == '/' && j + 1 < s.size() && (s[j + 1] == '/' || s[j + 1] == '*')) break;
             j++;
         }
+        if (j == i) j = i + 1;  // a character no token rule takes: returned alone, never stuck on it
         std::string out = s.substr(i, j - i);
         i = j;
         return out;
@@ -112,28 +117,62 @@ std::string dirname_of(const std::string& p) {
     return k == std::string::npos ? std::string(".") : p.substr(0, k);
 }
 
+// Text that is not a dictionary: a NUL or another control character
+// (OpenFOAM files are plain text; tabs, line and page breaks are whitespace).
+bool has_control_characters(const std::string& t) {
+    for (unsigned char c : t)
+        if ((c < 0x20 && !std::isspace(c)) || c == 0x7f) return true;
+    return false;
+}
+
+// `N ( ... )` with an integer N: OpenFOAM's sized list, whose size must be N
+bool sized_list_mismatch(const std::vector<NodeP>& items) {
+    if (items.size() < 2) return false;
+    const Node* c = items[items.size() - 2].get();
+    const Node* l = items.back().get();
+    if (c->kind != Node::TOKEN || c->quoted || l->kind != Node::LIST || c->tok.empty()) return false;
+    for (char ch : c->tok) if (!std::isdigit((unsigned char)ch)) return false;
+    return std::strtoul(c->tok.c_str(), nullptr, 10) != l->items.size();
+}
+
 struct Parser {
     std::string err;
     bool followIncludes = true;
+    int depth = 0;                        // nesting of lists and dictionaries
+    static constexpr int kMaxDepth = 256;
 
     NodeP parse_list(Lexer& L) {  // after '('
         auto n = std::make_shared<Node>();
         n->kind = Node::LIST;
+        if (++depth > kMaxDepth) { err = "lists nested too deeply"; --depth; return n; }
         for (;;) {
-            if (L.eof()) { err = "unterminated list"; return n; }
+            if (L.eof()) { err = "unterminated list"; break; }
             bool q = false;
             std::string t = L.next(&q);
-            if (!q && t == ")") return n;
-            if (!q && t == "(") { n->items.push_back(parse_list(L)); continue; }
+            if (!q && t == ")") break;
+            if (!q && t == "(") {
+                n->items.push_back(parse_list(L));
+                if (!err.empty()) break;
+                if (sized_list_mismatch(n->items)) { err = "list size differs from its count"; break; }
+                continue;
+            }
             auto tk = std::make_shared<Node>();
             tk->tok = t;
             tk->quoted = q;
             n->items.push_back(tk);
         }
+        --depth;
+        return n;
     }
 
     // parse dictionary entries until '}' (or EOF when top)
     void parse_dict(Lexer& L, Node& d, bool top) {
+        if (++depth > kMaxDepth) { err = "dictionaries nested too deeply"; --depth; return; }
+        parse_entries(L, d, top);
+        --depth;
+    }
+
+    void parse_entries(Lexer& L, Node& d, bool top) {
         for (;;) {
             if (L.eof()) {
                 if (!top) err = "unterminated dictionary";
@@ -153,8 +192,10 @@ struct Parser {
                 std::string path = (f.size() && f[0] == '/') ? f : L.dir + "/" + f;
                 std::string text;
                 if (!read_file(path, text)) continue;  // missing include: the keys it held stay absent
+                if (has_control_characters(text)) { err = "control character in " + path; return; }
                 Lexer sub(text, dirname_of(path));
                 parse_dict(sub, d, true);
+                if (err.empty() && !sub.bad.empty()) err = sub.bad + " in " + path;
                 if (!err.empty()) return;
                 continue;
             }
@@ -179,7 +220,12 @@ struct Parser {
                 bool q3 = false;
                 std::string t = L.next(&q3);
                 if (!q3 && t == ";") break;
-                if (!q3 && t == "(") { val->items.push_back(parse_list(L)); continue; }
+                if (!q3 && t == "(") {
+                    val->items.push_back(parse_list(L));
+                    if (!err.empty()) return;
+                    if (sized_list_mismatch(val->items)) { err = "list size differs from its count in " + key; return; }
+                    continue;
+                }
                 if (!q3 && t == "}") { err = "unexpected } in value of " + key; return; }
                 if (!q3 && t == "{") {
                     // uniform list N{v}: N copies of one element (thermo databases
@@ -190,7 +236,10 @@ struct Parser {
                     bool q4 = false;
                     std::string e = L.next(&q4);
                     NodeP elem;
-                    if (!q4 && e == "(") elem = parse_list(L);
+                    if (!q4 && e == "(") {
+                        elem = parse_list(L);
+                        if (!err.empty()) return;
+                    }
                     else { elem = std::make_shared<Node>(); elem->tok = e; elem->quoted = q4; }
                     if (L.next() != "}") { err = "bad uniform list in " + key; return; }
                     auto lst = std::make_shared<Node>();
@@ -211,9 +260,11 @@ struct Parser {
     bool parse_file(const std::string& path, Node& root) {
         std::string text;
         if (!read_file(path, text)) { err = "cannot read " + path; return false; }
+        if (has_control_characters(text)) { err = "control character in " + path; return false; }
         root.kind = Node::DICT;
         Lexer L(text, dirname_of(path));
         parse_dict(L, root, true);
+        if (err.empty() && !L.bad.empty()) err = L.bad;
         return err.empty();
     }
 };
@@ -260,11 +311,15 @@ bool list_doubles(const Node* l, std::vector<double>& out) {
 
 namespace {
 
+// Largest stoichiometric coefficient the reader expands (each unit is one
+// species entry of the reaction; the GPU takes at most 4 reactant and 8
+// product entries, fcs_load_mechanism refuses more).
+constexpr int kMaxCoefficient = 64;
+
 // Parses the reactions and thermo files into a flat description and hands it
 // (with the species names) to visit; the arrays live until visit returns.
-fcs_status parse_foam(const char* reactions_path, const char* thermo_path, fcs_mechanism_visitor visit,
-                      void* user) {
-    if (!reactions_path || !thermo_path || !visit) return FCS_ERR_INVALID;
+fcs_status parse_foam_files(const char* reactions_path, const char* thermo_path, fcs_mechanism_visitor visit,
+                            void* user) {
     Parser P;
     Node rfile, tfile;
     if (!P.parse_file(reactions_path, rfile)) return FCS_ERR_PARSE;
@@ -332,23 +387,35 @@ fcs_status parse_foam(const char* reactions_path, const char* thermo_path, fcs_m
         int eqpos = -1;
         for (int k = 0; k < (int)words.size(); k++) if (words[k] == "=") eqpos = k;
         if (eqpos < 0) return FCS_ERR_PARSE;
+        // Each side is one or more terms joined by '+' (the reference skips
+        // every '+' and would take "A + = B" or "= B" too; a side without a
+        // species, or a dangling '+', is refused here).
         auto side = [&](int k0, int k1, std::vector<int32_t>& out) -> bool {
+            bool expectTerm = true;
             for (int k = k0; k < k1; k++) {
-                if (words[k] == "+") continue;
+                if (words[k] == "+") {
+                    if (expectTerm) return false;
+                    expectTerm = true;
+                    continue;
+                }
+                if (!expectTerm) return false;
+                expectTerm = false;
                 const std::string& t = words[k];
                 size_t first = 0;
                 while (first < t.size() && (std::isdigit((unsigned char)t[first]) || t[first] == '.')) first++;
                 int coef = 1;
                 if (first > 0) {
-                    const double v = std::stod(t.substr(0, first));
-                    if (v != std::floor(v) || v < 0) return false;
+                    char* end = nullptr;
+                    const std::string num = t.substr(0, first);
+                    const double v = std::strtod(num.c_str(), &end);
+                    if (!end || *end || v != std::floor(v) || v < 1 || v > kMaxCoefficient) return false;
                     coef = (int)v;
                 }
                 auto it = index.find(t.substr(first));
                 if (it == index.end()) return false;
                 for (int c = 0; c < coef; c++) out.push_back(it->second);
             }
-            return true;
+            return !expectTerm;
         };
         if (!side(0, eqpos, ls) || !side(eqpos + 1, (int)words.size(), rs)) return FCS_ERR_PARSE;
         lo.push_back((int32_t)ls.size());
@@ -373,6 +440,10 @@ fcs_status parse_foam(const char* reactions_path, const char* thermo_path, fcs_m
                 return FCS_ERR_PARSE;
         }
         arr2.push_back(kA); arr2.push_back(kb); arr2.push_back(kt);
+        // Third-body efficiencies: required where the reference looks them up
+        // (OptReaction.C:669, 724, 776, 830, 889); species the list leaves out
+        // keep efficiency 1 (the reference indexes its table by species and
+        // needs every species listed).
         std::vector<double> row(ns, 1.0);
         const Node* cnode = nullptr;
         if (kind == FCS_RXN_THIRD_BODY) cnode = r->find("coeffs");
@@ -381,8 +452,11 @@ fcs_status parse_foam(const char* reactions_path, const char* thermo_path, fcs_m
         else if (kind == FCS_RXN_NONEQ_THIRD_BODY) cnode = k0->find("coeffs");
         else if (falloff) {
             const Node* tb = r->find("thirdBodyEfficiencies");
-            if (tb) cnode = tb->find("coeffs");
+            if (!tb || tb->kind != Node::DICT) return FCS_ERR_PARSE;
+            cnode = tb->find("coeffs");
         }
+        const bool needsEfficiencies = kind == FCS_RXN_THIRD_BODY || kind == FCS_RXN_NONEQ_THIRD_BODY || falloff;
+        if (needsEfficiencies && !cnode) return FCS_ERR_PARSE;
         if (cnode) {
             const Node* l = inner_list(cnode);
             if (!l) return FCS_ERR_PARSE;
@@ -395,14 +469,18 @@ fcs_status parse_foam(const char* reactions_path, const char* thermo_path, fcs_m
             }
         }
         eff.insert(eff.end(), row.begin(), row.end());
+        // Troe (alpha, Ts, Tss, Tsss) and SRI (a..e) parameters: all required,
+        // as the reference's lookups (OptReaction.C:841-844, 900-904)
         double f5[5] = {0, 0, 0, 0, 0};
         const Node* F = r->find("F");
-        if (F && kind == FCS_RXN_TROE_FALLOFF) {
-            as_double(F->find("alpha"), f5[0]); as_double(F->find("Ts"), f5[1]);
-            as_double(F->find("Tss"), f5[2]); as_double(F->find("Tsss"), f5[3]);
-        } else if (F && kind == FCS_RXN_SRI_FALLOFF) {
-            as_double(F->find("a"), f5[0]); as_double(F->find("b"), f5[1]); as_double(F->find("c"), f5[2]);
-            as_double(F->find("d"), f5[3]); as_double(F->find("e"), f5[4]);
+        if (kind == FCS_RXN_TROE_FALLOFF) {
+            if (!F || !as_double(F->find("alpha"), f5[0]) || !as_double(F->find("Ts"), f5[1]) ||
+                !as_double(F->find("Tss"), f5[2]) || !as_double(F->find("Tsss"), f5[3]))
+                return FCS_ERR_PARSE;
+        } else if (kind == FCS_RXN_SRI_FALLOFF) {
+            if (!F || !as_double(F->find("a"), f5[0]) || !as_double(F->find("b"), f5[1]) ||
+                !as_double(F->find("c"), f5[2]) || !as_double(F->find("d"), f5[3]) || !as_double(F->find("e"), f5[4]))
+                return FCS_ERR_PARSE;
         }
         fp.insert(fp.end(), f5, f5 + 5);
         int rows = 0;
@@ -434,6 +512,20 @@ fcs_status parse_foam(const char* reactions_path, const char* thermo_path, fcs_m
     return visit(&d, names.data(), user);
 }
 
+// No C++ exception crosses the C ABI: a file the reader cannot take is
+// FCS_ERR_PARSE, running out of host memory FCS_ERR_NOMEM.
+fcs_status parse_foam(const char* reactions_path, const char* thermo_path, fcs_mechanism_visitor visit,
+                      void* user) {
+    if (!reactions_path || !thermo_path || !visit) return FCS_ERR_INVALID;
+    try {
+        return parse_foam_files(reactions_path, thermo_path, visit, user);
+    } catch (const std::bad_alloc&) {
+        return FCS_ERR_NOMEM;
+    } catch (...) {
+        return FCS_ERR_PARSE;
+    }
+}
+
 fcs_status load_visitor(const fcs_mechanism_desc* d, const char* const*, void* ctx) {
     return fcs_load_mechanism(static_cast<fcs_ctx*>(ctx), d);
 }
@@ -450,8 +542,17 @@ extern "C" fcs_status fcs_parse_mechanism_foam(const char* reactions_path, const
     return parse_foam(reactions_path, thermo_path, visit, user);
 }
 
-extern "C" fcs_status fcs_read_chemistry_properties(const char* path, fcs_options* o, double* initial_sub_dt) {
-    if (!path || !o) return FCS_ERR_INVALID;
+namespace {
+
+// A positive whole number that fits an int32 (maxSteps, maxRejects)
+bool as_count(const Node* v, int32_t& out) {
+    double d;
+    if (!as_double(v, d) || !(d >= 1) || d > 2147483647.0 || d != std::floor(d)) return false;
+    out = (int32_t)d;
+    return true;
+}
+
+fcs_status read_chemistry_properties(const char* path, fcs_options* o, double* initial_sub_dt) {
     Parser P;
     P.followIncludes = false;  // `#include "reactions"` carries no solver keys
     Node root;
@@ -480,7 +581,7 @@ extern "C" fcs_status fcs_read_chemistry_properties(const char* path, fcs_option
     if (!cd || cd->kind != Node::DICT) return FCS_ERR_PARSE;  // absTol/relTol are required
     if (!as_double(cd->find("absTol"), o->abs_tol) || !as_double(cd->find("relTol"), o->rel_tol))
         return FCS_ERR_PARSE;
-    if (as_double(cd->find("maxSteps"), v)) o->max_steps = (int32_t)v;
+    if (cd->find("maxSteps") && !as_count(cd->find("maxSteps"), o->max_steps)) return FCS_ERR_PARSE;
     const Node* gd = root.find("FastChemistryGPU");
     if (gd && gd->kind == Node::DICT) {
         std::string w;
@@ -498,7 +599,20 @@ extern "C" fcs_status fcs_read_chemistry_properties(const char* path, fcs_option
             else if (w == "block256") o->mapping = FCS_MAPPING_BLOCK256;
             else return FCS_ERR_PARSE;
         }
-        if (as_double(gd->find("maxRejects"), v)) o->max_rejects = (int32_t)v;
+        if (gd->find("maxRejects") && !as_count(gd->find("maxRejects"), o->max_rejects)) return FCS_ERR_PARSE;
     }
     return FCS_OK;
+}
+
+}  // namespace
+
+extern "C" fcs_status fcs_read_chemistry_properties(const char* path, fcs_options* o, double* initial_sub_dt) {
+    if (!path || !o) return FCS_ERR_INVALID;
+    try {
+        return read_chemistry_properties(path, o, initial_sub_dt);
+    } catch (const std::bad_alloc&) {
+        return FCS_ERR_NOMEM;
+    } catch (...) {
+        return FCS_ERR_PARSE;
+    }
 }

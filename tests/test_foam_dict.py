@@ -120,3 +120,131 @@ reactions
     np.testing.assert_array_equal(b.rhs_species, [1, 2, 1, 1])
     np.testing.assert_array_equal(b.arrhenius, [7e9, 0, 0, 1e10, 0.5, 100])
     np.testing.assert_allclose(b.W, [14.027, 14.027, 2.016])
+
+
+# ---------------------------------------------------------------------------
+# Files the reader must refuse (FCS_ERR_PARSE, or FCS_ERR_UNSUPPORTED for a
+# reaction type it does not implement) without crashing or hanging: the flow
+# solver hands the library whatever its case directory holds.
+
+FCS_ERR_UNSUPPORTED = 6
+FCS_ERR_PARSE = 7
+
+_NASA = "( 3.5 0.001 0 0 0 -1000 3 )"
+_THERMO = "species 3 ( A B C );\n" + "".join(
+    f"{s} {{ specie {{ molWeight {w}; }} thermodynamics {{ Tlow 200; Thigh 3500; Tcommon 1000; "
+    f"highCpCoeffs {_NASA}; lowCpCoeffs {_NASA}; }} }}\n" for s, w in (("A", 10), ("B", 20), ("C", 30)))
+_ARR = "A 1e10; beta 0; Ta 100;"
+_TBE = "thirdBodyEfficiencies { coeffs 3 ( (A 1) (B 2) (C 3) ); }"
+_K = "k0 { A 1; beta 0; Ta 0; } kInf { A 2; beta 0; Ta 0; }"
+
+
+def _reactions(body):
+    return "reactions\n{\n    r0\n    {\n        " + body + "\n    }\n}\n"
+
+
+def _parse(tmp_path, reactions, thermo=_THERMO):
+    r, t = tmp_path / "reactions", tmp_path / "thermo"
+    r.write_text(reactions)
+    t.write_text(thermo)
+    return _lib.parse_mechanism_foam(str(r), str(t))
+
+
+_REFUSED = {
+    "empty reactions file": ("", _THERMO),
+    "no reactions dictionary": ("foo { }\n", _THERMO),
+    "reactions as a list": ("reactions ( );\n", _THERMO),
+    "unknown species": (_reactions(f'type reversibleArrhenius; reaction "X + B = C"; {_ARR}'), _THERMO),
+    "empty term": (_reactions(f'type reversibleArrhenius; reaction "A + = C"; {_ARR}'), _THERMO),
+    "no reactants": (_reactions(f'type reversibleArrhenius; reaction "= C"; {_ARR}'), _THERMO),
+    "no products": (_reactions(f'type reversibleArrhenius; reaction "A ="; {_ARR}'), _THERMO),
+    "leading +": (_reactions(f'type reversibleArrhenius; reaction "+ A = C"; {_ARR}'), _THERMO),
+    "double +": (_reactions(f'type reversibleArrhenius; reaction "A + + B = C"; {_ARR}'), _THERMO),
+    "no =": (_reactions(f'type reversibleArrhenius; reaction "A B C"; {_ARR}'), _THERMO),
+    "two =": (_reactions(f'type reversibleArrhenius; reaction "A = B = C"; {_ARR}'), _THERMO),
+    "negative coefficient": (_reactions(f'type reversibleArrhenius; reaction "-1A = C"; {_ARR}'), _THERMO),
+    "fractional coefficient": (_reactions(f'type reversibleArrhenius; reaction "0.5A = C"; {_ARR}'), _THERMO),
+    "coefficient without digits": (_reactions(f'type reversibleArrhenius; reaction ".A = C"; {_ARR}'), _THERMO),
+    "coefficient out of range": (_reactions(f'type reversibleArrhenius; reaction "99999999999999999999A = C"; {_ARR}'),
+                                 _THERMO),
+    "reaction order syntax": (_reactions(f'type reversibleArrhenius; reaction "A^2 = C"; {_ARR}'), _THERMO),
+    "missing A": (_reactions('type reversibleArrhenius; reaction "A + B = C"; beta 0; Ta 0;'), _THERMO),
+    "A not a number": (_reactions('type reversibleArrhenius; reaction "A + B = C"; A abc; beta 0; Ta 0;'), _THERMO),
+    "third body without coeffs": (_reactions(f'type reversibleThirdBodyArrhenius; reaction "A + B = C"; {_ARR}'),
+                                  _THERMO),
+    "sized list of the wrong size": (_reactions(f'type reversibleThirdBodyArrhenius; reaction "A + B = C"; {_ARR} '
+                                                'coeffs 3 ( (A 1) (B 1) );'), _THERMO),
+    "fall-off without efficiencies": (_reactions(f'type reversibleArrheniusLindemannFallOff; reaction "A + B = C"; {_K}'),
+                                      _THERMO),
+    "Troe without F": (_reactions(f'type reversibleArrheniusTroeFallOff; reaction "A + B = C"; {_K} {_TBE}'), _THERMO),
+    "SRI without e": (_reactions(f'type reversibleArrheniusSRIFallOff; reaction "A + B = C"; {_K} '
+                                 f'F {{ a 1; b 2; c 3; d 1; }} {_TBE}'), _THERMO),
+    "PLOG without rows": (_reactions('type reversibleArrheniusPLOG; reaction "A + B = C"; ArrheniusData ( );'),
+                          _THERMO),
+    "PLOG row of three": (_reactions('type reversibleArrheniusPLOG; reaction "A + B = C"; ArrheniusData ( (1e5 1 0) );'),
+                          _THERMO),
+    "truncated file": (_reactions(f'type reversibleArrhenius; reaction "A + B = C"; {_ARR}')[:-10], _THERMO),
+    "unterminated string": (_reactions(f'type reversibleArrhenius; reaction "A + B = C; {_ARR}'), _THERMO),
+    "unterminated comment": (_reactions(f'type reversibleArrhenius; reaction "A + B = C"; {_ARR}') + "/* open",
+                             _THERMO),
+    "unbalanced }": ("reactions\n{\n}\n}\n", _THERMO),
+    "NUL bytes": ("reactions { r0 { type \0\0\0; } }\n", _THERMO),
+    "nested too deeply": ("reactions\n" + "{ a\n" * 5000 + "}\n" * 5000, _THERMO),
+    "thermo missing a listed species": (_reactions(f'type reversibleArrhenius; reaction "A + B = C"; {_ARR}'),
+                                        _THERMO.replace("species 3 ( A B C );", "species 4 ( A B C D );")),
+    "species list of the wrong size": (_reactions(f'type reversibleArrhenius; reaction "A + B = C"; {_ARR}'),
+                                       _THERMO.replace("species 3 ( A B C );", "species 5 ( A B C );")),
+    "six NASA coefficients": (_reactions(f'type reversibleArrhenius; reaction "A + B = C"; {_ARR}'),
+                              _THERMO.replace(_NASA, "( 3.5 0.001 0 0 0 -1000 )", 1)),
+    "empty thermo": (_reactions(f'type reversibleArrhenius; reaction "A + B = C"; {_ARR}'), ""),
+}
+
+
+@pytest.mark.parametrize("case", list(_REFUSED), ids=list(_REFUSED))
+def test_reader_refuses_malformed_files(tmp_path, lib_path, case):
+    reactions, thermo = _REFUSED[case]
+    with pytest.raises(_lib.FcsError) as e:
+        _parse(tmp_path, reactions, thermo)
+    assert e.value.code == FCS_ERR_PARSE
+
+
+def test_reader_refuses_unknown_reaction_types(tmp_path, lib_path):
+    for t in ("fooArrhenius", "reversibleArrheniusTroeChemicallyActivated", "irreversibleLandauTellerReaction"):
+        with pytest.raises(_lib.FcsError) as e:
+            _parse(tmp_path, _reactions(f'type {t}; reaction "A + B = C"; {_ARR}'))
+        assert e.value.code == FCS_ERR_UNSUPPORTED, t
+
+
+def test_reader_takes_the_well_formed_neighbours(tmp_path, lib_path):
+    """The same files, well formed: the fall-off parameters, a third-body list
+    that leaves species out (they keep efficiency 1), integer coefficients,
+    and more species than the GPU takes (the loader, not the reader, refuses
+    those)."""
+    import numpy as np
+    troe = _reactions(f'type reversibleArrheniusTroeFallOff; reaction "A + B = C"; {_K} '
+                      f'F {{ alpha 0.5; Tsss 100; Ts 1000; Tss 5000; }} {_TBE}')
+    b, _ = _parse(tmp_path, troe)
+    np.testing.assert_array_equal(b.falloff_params, [0.5, 1000, 5000, 100, 0])
+    np.testing.assert_array_equal(b.efficiencies, [1, 2, 3])
+    tb = _reactions(f'type reversibleThirdBodyArrhenius; reaction "2A + B = 3C"; {_ARR} coeffs 2 ( (B 2.5) (C 4) );')
+    b, _ = _parse(tmp_path, tb)
+    np.testing.assert_array_equal(b.efficiencies, [1, 2.5, 4])
+    np.testing.assert_array_equal(b.lhs_species, [0, 0, 1])
+    np.testing.assert_array_equal(b.rhs_species, [2, 2, 2])
+    many = "species 300 (" + " ".join(f"S{i}" for i in range(300)) + ");\n" + "".join(
+        f"S{i} {{ specie {{ molWeight 10; }} thermodynamics {{ Tlow 200; Thigh 3500; Tcommon 1000; "
+        f"highCpCoeffs {_NASA}; lowCpCoeffs {_NASA}; }} }}\n" for i in range(300))
+    b, names = _parse(tmp_path, _reactions(f'type reversibleArrhenius; reaction "S0 + S1 = S299"; {_ARR}'), many)
+    assert b.n_species == 300 and names[-1] == "S299"
+
+
+def test_chemistry_properties_refuses_bad_counts(tmp_path, lib_path):
+    for bad in ("maxSteps -5;", "maxSteps 1e12;", "maxSteps 2.5;", "maxSteps abc;"):
+        p = tmp_path / "cp"
+        p.write_text(f"chemistryType {{ solver OptRodas34; }}\nOptRodas34Coeffs {{ absTol 1e-8; relTol 1e-4; {bad} }}\n")
+        with pytest.raises(_lib.FcsError) as e:
+            _lib.read_chemistry_properties(str(p))
+        assert e.value.code == FCS_ERR_PARSE, bad
+    p.write_text("chemistryType { solver OptRodas34; }\nOptRodas34Coeffs { absTol 1e-8; relTol 1e-4; maxSteps 1e6; }\n")
+    o, _ = _lib.read_chemistry_properties(str(p))
+    assert o.max_steps == 1000000
