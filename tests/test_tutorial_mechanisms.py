@@ -108,3 +108,28 @@ def test_tutorial_mechanism_oracle_matches_reference(ref_available, case, fuel):
     np.testing.assert_allclose(r1["T"], r0["T"], rtol=1e-8)
     np.testing.assert_allclose(r1["Y"], r0["Y"], atol=1e-9)
     assert abs(r1["counters"]["jacobians"] - r0["counters"]["jacobians"]) <= 2
+
+
+SOLVER_MECHS = [("Ignition0D/CH4_GRI30", "CH4"), ("CounterFlowFlame2D/NH3_Zhang", "NH3"),
+                ("Ignition0D/H2_Connaire2004", "h2")]
+
+
+@pytest.mark.parametrize("solver", ["OptRosenbrock34", "OptRodas23", "OptRosenbrock23", "OptSeulex"])
+@pytest.mark.parametrize("case,fuel", SOLVER_MECHS, ids=[m[0].split("/")[1] for m in SOLVER_MECHS])
+def test_tutorial_mechanism_other_solvers(ref_available, case, fuel, solver):
+    """The other registered solvers on real mechanisms (fall-off and CH2(S)
+    in GRI-3.0, PLOG in NH3_Zhang, non-equilibrium third-body reactions in
+    H2_Connaire2004): one 1e-5 s CFD step of ignition-like cells, the oracle
+    against the reference core compiled from its sources."""
+    import oracle
+    from fcs import _lib
+    rpath, tpath = _files(case)
+    flat, names = _lib.parse_mechanism_foam(rpath, tpath)
+    c = _cells(flat, names, fuel, 3, seed=len(names) + 1)
+    r0 = oracle.Reference(flat, solver=solver, abs_tol=1e-8, rel_tol=1e-4).integrate(c, 1e-5)
+    r1 = oracle.Port(flat).integrate(c, 1e-5, solver=solver, abs_tol=1e-8, rel_tol=1e-4)
+    assert (r0["status"] == 0).all() and (r1["status"] == 0).all()
+    np.testing.assert_allclose(r1["T"], r0["T"], rtol=1e-8)
+    np.testing.assert_allclose(r1["Y"], r0["Y"], atol=1e-9)
+    # Seulex may take one ulp-level extra step at the end of the interval
+    assert abs(r1["counters"]["jacobians"] - r0["counters"]["jacobians"]) <= (3 if solver == "OptSeulex" else 2)
