@@ -126,6 +126,34 @@ def test_port_against_compiled_reference_directly(port_built):
     np.testing.assert_allclose(r1["Y"], r0["Y"], atol=1e-9)
 
 
+@pytest.mark.parametrize("wname", ["counterflow_53s", "falloff_16s", "noneq_14s"])
+def test_port_fast_jacobian_against_compiled_reference(wname, port_built):
+    """`jacobian fast` (FastddYdtdY_Vec, Jacobian.C:4541-4568: the dC/dY
+    conversion without the rank-1 term): the oracle's Jacobian and a CFD step
+    integrated with it, against the reference core compiled from its sources."""
+    import oracle
+    if not os.path.exists(oracle.REF_SO):
+        pytest.skip("reference core not built on this host")
+    w = fcs.WORKLOADS[wname]
+    mech = w.mechanism()
+    flat = fcs.flatten(mech)
+    cells = fcs.cells_for(w, mech, n=64).subset(np.arange(0, 64, 16))
+    ref = oracle.Reference(flat, jacobian="fast", abs_tol=w.abs_tol, rel_tol=w.rel_tol)
+    port = oracle.Port(flat)
+    J0, _ = ref.jacobian(cells.p, cells.T, cells.Y)
+    J1, _ = port.jacobian(cells.p, cells.T, cells.Y, jacobian="fast")
+    Je, _ = port.jacobian(cells.p, cells.T, cells.Y)
+    scale = np.abs(J0).max(axis=(1, 2), keepdims=True)
+    assert np.max(np.abs(J1 - J0) / scale) < 1e-12
+    assert np.max(np.abs(Je - J0) / scale) > 1e-9  # the exact conversion differs: the mode took effect
+    r0 = ref.integrate(cells, w.dt, treact=w.treact)
+    r1 = port.integrate(cells, w.dt, jacobian="fast", abs_tol=w.abs_tol, rel_tol=w.rel_tol, treact=w.treact)
+    assert (r0["status"] == r1["status"]).all()
+    np.testing.assert_allclose(r1["T"], r0["T"], rtol=1e-8)
+    np.testing.assert_allclose(r1["Y"], r0["Y"], atol=1e-9)
+    assert abs(int(r1["counters"]["jacobians"]) - int(r0["counters"]["jacobians"])) <= 2 * cells.n
+
+
 @pytest.mark.parametrize("wname", ["ignition_10s", "counterflow_53s", "uneven_111s", "falloff_16s", "noneq_14s", "long_24s"])
 def test_port_tc_matches_reference_golden(wname, port_built):
     """FastChemistryModel::tc() of the reference (tests/golden/tc.npz)."""
