@@ -11,6 +11,8 @@ import fcs
 from conftest import GOLDEN
 from golden import fixture
 
+FCS_CELL_MAX_STEPS = 1
+
 
 def _golden(name):
     return np.load(os.path.join(GOLDEN, name + ".npz"))
@@ -152,6 +154,35 @@ def test_port_fast_jacobian_against_compiled_reference(wname, port_built):
     np.testing.assert_allclose(r1["T"], r0["T"], rtol=1e-8)
     np.testing.assert_allclose(r1["Y"], r0["Y"], atol=1e-9)
     assert abs(int(r1["counters"]["jacobians"]) - int(r0["counters"]["jacobians"])) <= 2 * cells.n
+
+
+@pytest.mark.parametrize("solver", ["OptRodas34", "OptSeulex"])
+def test_port_max_steps_status_against_compiled_reference(solver, port_built):
+    """maxSteps, the reference's only failure path (FatalError at
+    OptRodas34.C:193, OptSeulex.C:252): with a step budget that only some of
+    the cells finish in, the oracle fails exactly the cells the reference
+    core fails, and the others finish as in the reference."""
+    import oracle
+    if not os.path.exists(oracle.REF_SO):
+        pytest.skip("reference core not built on this host")
+    w = fcs.WORKLOADS["counterflow_53s"]
+    mech = w.mechanism()
+    flat = fcs.flatten(mech)
+    cells = fcs.cells_for(w, mech).subset(np.linspace(0, w.n_cells - 1, 12).astype(np.int64))
+    # the smallest of these budgets that some but not all of the cells finish in
+    for steps in (8, 16, 32, 64, 128, 256):
+        ref = oracle.Reference(flat, solver=solver, abs_tol=w.abs_tol, rel_tol=w.rel_tol, max_steps=steps)
+        r0 = ref.integrate(cells, w.dt)
+        failed = r0["status"] == FCS_CELL_MAX_STEPS
+        if failed.any() and not failed.all():
+            break
+    assert failed.any() and not failed.all(), r0["status"]
+    r1 = oracle.Port(flat).integrate(cells, w.dt, solver=solver, abs_tol=w.abs_tol, rel_tol=w.rel_tol,
+                                     max_steps=steps)
+    np.testing.assert_array_equal(r1["status"], r0["status"])
+    ok = ~failed  # the 53-species tolerances of the golden comparisons (libm vs libmvec exp, sum order)
+    np.testing.assert_allclose(r1["T"][ok], r0["T"][ok], rtol=1e-7)
+    np.testing.assert_allclose(r1["Y"][:, ok], r0["Y"][:, ok], atol=1e-8)
 
 
 @pytest.mark.parametrize("wname", ["ignition_10s", "counterflow_53s", "uneven_111s", "falloff_16s", "noneq_14s", "long_24s"])
